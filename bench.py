@@ -1,0 +1,370 @@
+#!/usr/bin/env python
+"""FWI shot-gradient throughput of the GB300 engine (one JSON line on rank 0).
+
+Workload: the batched Marmousi-like gradient -- 481 x 141 grid at 25 m, 40-point
+PML, nt = 4000, dt = 2 ms, 49 shots at z = 25 m, 481 surface receivers, 5 Hz
+Ricker -- on a seeded synthetic faulted-layer model (no public model is read).
+One step = one Waveform-misfit gradient of every shot: forward with boundary
+strips, adjoint source syn - obs, reconstruction + adjoint + imaging, shot sum.
+
+  value  shot-gradients/s with inputs resident in device memory
+  e2e    the same through the C ABI with host (pinned) buffers: model, sources and
+         observed data copied in, gradient + illuminations + misfit copied out
+         every step
+Under torchrun (N > 1) every rank runs its own 49-shot block of a 49 N-shot
+survey and the gradients are summed with one all-reduce (weak scaling).
+``--impl reference`` times the CPU restatement of fd2dmpi (the reference's
+Fortran cannot be built here) on the host cores instead.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "FWI shot-gradients/s (481x141, nt=4000) batched vs plain GPU; GPts/s, % HBM roof"
+UNIT = "shot-gradients/s"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="mine", choices=["mine", "reference"])
+    ap.add_argument("--shots", type=int, default=None, help="shots per rank (default 49)")
+    ap.add_argument("--nt", type=int, default=None, help="time steps (default 4000)")
+    ap.add_argument("--batch", type=int, default=0, help="shots per launch (0 = engine default)")
+    ap.add_argument("--block-x", type=int, default=0)
+    ap.add_argument("--no-extras", action="store_true", help="skip plain path, CPU baseline and kernel profile")
+    return ap.parse_args()
+
+
+# --------------------------------------------------------------------- units
+def work_units(nx, nz, npml, nt, ng):
+    """Grid-point updates U and algorithmic bytes B per shot-gradient.
+
+    U = (nt-1) (2 N_pml + N_int); B = (nt-1) [64 N_pml + 56 N_int + 8 S] + 8 nt ng
+    with N_pml = (nx+2 npml)(nz+2 npml), N_int = nx nz, S = 9 nx + 6 nz: state
+    p, u, w read and written once per step on the PML grid forward and adjoint,
+    two coefficient arrays, the interior reconstruction and three imaging sums,
+    strips written and read, seismograms written and adjoint sources read.
+    """
+    npml_pts = (nx + 2 * npml) * (nz + 2 * npml)
+    nint = nx * nz
+    S = 9 * nx + 6 * nz
+    U = (nt - 1) * (2 * npml_pts + nint)
+    B = (nt - 1) * (64 * npml_pts + 56 * nint + 8 * S) + 8 * nt * ng
+    return U, B
+
+
+def kernel_bytes_per_shot(nx, nz, npml, ng):
+    """Compulsory bytes one launch of each stencil kernel moves per shot (each
+    array it touches read or written once, neighbours not counted again)."""
+    npts = (nx + 2 * npml) * (nz + 2 * npml)
+    nint = nx * nz
+    return {
+        "fwd_p": 20 * npts,                                   # p r/w, u, w, A
+        "fwd_uw": 24 * npts + 4 * (9 * nx + 6 * nz) + 4 * ng,  # u, w r/w, p, B; strips, trace samples
+        "bwd_uw": 24 * npts + 24 * nint + 4 * (nx + 2 * nz),   # adjoint u, w; reconstruction u, w; strips
+        "bwd_p": 20 * npts + 44 * nint + 4 * (5 * nx + 4 * nz) + 4 * ng,  # adjoint p; reco p; imaging; strips
+    }
+
+
+def measured_peak():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def ncu_traffic():
+    """DRAM bytes per shot and launch of each stencil kernel from the committed
+    ncu summary (profiles/stencil_traffic.txt), or {} if there is none."""
+    p = os.path.join(ROOT, "profiles", "stencil_traffic.txt")
+    out = {}
+    if os.path.exists(p):
+        for line in open(p):
+            if line.startswith("traffic "):
+                kv = dict(x.split("=", 1) for x in line.split()[1:])
+                out[kv["kernel"]] = float(kv["bytes_per_shot_launch"])
+    return out
+
+
+# --------------------------------------------------------------------- clocks
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.thread.join(timeout=2)
+        sm, smax, reasons = [], [], set()
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(smax)), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# --------------------------------------------------------------------- arms
+def cpu_baseline(sv, rho, src, obs, threads, kind="port"):
+    """Oracle (C++ restatement of fd2dmpi, FP32, -O3, one shot per thread with
+    fd2dmpi's static shot split) on min(ns, threads) shots at full nt."""
+    from oracle import oracle as O
+    n = min(sv.ns, threads)
+    pb = O.Problem(sv.nx, sv.nz, sv.npml, sv.nt, sv.dx, sv.dt, sv.src_xz[:n], sv.rec_xz[:n])
+    t0 = time.perf_counter()
+    O.gradient(pb, sv.vp_init, rho, src[:n], obs[:n], nthreads=threads)
+    wall = time.perf_counter() - t0
+    return {"value": n / wall, "unit": UNIT, "cores": threads, "kind": kind,
+            "sample": "%d of %d shots at full nt=%d, one shot per thread, %.1f s wall" % (n, sv.ns, sv.nt, wall)}
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    from oracle import oracle as O
+    from swit_gb300 import survey
+    sv = survey.config(1, ns=args.shots, nt=args.nt)
+    threads = os.cpu_count() or 1
+    rho = sv.rho(sv.vp_true)
+    src = sv.source()
+    n = min(sv.ns, threads)
+    pb = O.Problem(sv.nx, sv.nz, sv.npml, sv.nt, sv.dx, sv.dt, sv.src_xz[:n], sv.rec_xz[:n])
+    obs = O.forward(pb, sv.vp_true, rho, src[:n], store=False, nthreads=threads)["seis"]
+    vals = []
+    for i in range(args.warmup + args.steps):
+        b = cpu_baseline(sv, rho, src, obs, threads, kind="port")
+        if i >= args.warmup:
+            vals.append(b["value"])
+    v = float(np.mean(vals))
+    U, B = work_units(sv.nx, sv.nz, sv.npml, sv.nt, sv.ng)
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * n / v,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": sv.name, "grid": [sv.nx, sv.nz], "npml": sv.npml, "nt": sv.nt, "shots": sv.ns,
+                       "receivers": sv.ng, "dx_m": sv.dx, "dt_s": sv.dt, "engine": "CPU restatement of fd2dmpi "
+                       "(oracle/fd2d_oracle.cpp, FP32, g++ -O3); fd2dmpi itself needs gfortran + MPI, absent"},
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": "%d of %d shots per step at full nt, one shot per thread" % (n, sv.ns)},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "gpts_per_s": v * U / 1e9}
+    print(json.dumps(line), flush=True)
+
+
+def run_mine(args):
+    import torch
+    import torch.distributed as dist
+
+    from swit_gb300 import Engine, survey
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    if world > 1:
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    per_rank = args.shots or 49
+    full = survey.config(1, ns=per_rank * world, nt=args.nt)
+    # rank r owns a contiguous block of shots (fd2dmpi/mmi_mpi.f90:52-80 with equal blocks)
+    lo, hi = rank * per_rank, (rank + 1) * per_rank
+    sv = full
+    src_xz, rec_xz = full.src_xz[lo:hi], full.rec_xz[lo:hi]
+    rho = sv.rho(sv.vp_true)
+    src = sv.source()[lo:hi].copy()
+    eng = Engine(sv.nx, sv.nz, sv.npml, sv.nt, sv.dx, sv.dt, src_xz, rec_xz, shots_per_batch=args.batch,
+                 block_x=args.block_x)
+    q = eng.query()
+    # observed data from the true model, synthetics from the smoothed model
+    eng.set_model(sv.vp_true, rho)
+    src_d = torch.from_numpy(src).cuda()
+    obs_d = eng.forward(src_d, save_boundary=False)
+    eng.set_model(sv.vp_init, rho)
+    torch.cuda.synchronize()
+
+    def step_device():
+        out = eng.gradient_l2(src_d, obs_d)
+        if world > 1:
+            for k in ("grad", "illum_fw", "illum_bk"):
+                dist.all_reduce(out[k])
+        return out
+
+    for _ in range(args.warmup):
+        step_device()
+    torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    clocks = ClockSampler(local)
+    clocks.start()
+    time.sleep(0.3)
+    stream = torch.cuda.current_stream()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    ev0.record(stream)
+    for _ in range(args.steps):
+        step_device()
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    ms = ev0.elapsed_time(ev1)
+    if world > 1:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+        dist.barrier()
+    ms_per_step = ms / args.steps
+    value = per_rank * world / (ms_per_step / 1000.0)
+
+    # ---- e2e: the same step through the C ABI with host buffers
+    src_h = torch.from_numpy(src).pin_memory()
+    obs_h = obs_d.cpu().pin_memory()
+    vp_h = torch.from_numpy(sv.vp_init).pin_memory()
+    rho_h = torch.from_numpy(rho).pin_memory()
+
+    def step_host():
+        eng.set_model(vp_h, rho_h)
+        out = eng.gradient_l2(src_h, obs_h)
+        if world > 1:
+            g = torch.from_numpy(np.stack([out["grad"], out["illum_fw"], out["illum_bk"]])).cuda()
+            dist.all_reduce(g)
+            g.cpu()
+        return out
+
+    for _ in range(max(1, args.warmup // 2)):
+        step_host()
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        step_host()
+    torch.cuda.synchronize()
+    e2e_s = (time.perf_counter() - t0) / args.steps
+    if world > 1:
+        t = torch.tensor([e2e_s], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    NX, LD = sv.nx + 2 * sv.npml, ((sv.nz + 2 * sv.npml + 31) // 32) * 32
+    LDI = ((sv.nz + 31) // 32) * 32
+    h2d = (2 * sv.nx * sv.nz * 4 + src.nbytes + obs_h.numel() * 4 + 2 * NX * LD * 4 + sv.nx * LDI * 4
+           + (sv.npml + 1) * 4)
+    d2h = 3 * sv.nx * sv.nz * 4 + per_rank * sv.ng * 8
+
+    U, B = work_units(sv.nx, sv.nz, sv.npml, sv.nt, sv.ng)
+    peak, peak_kind = measured_peak()
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": sv.name, "grid": [sv.nx, sv.nz], "npml": sv.npml, "nt": sv.nt,
+                       "shots_per_gpu": per_rank, "receivers": sv.ng, "dx_m": sv.dx, "dt_s": sv.dt,
+                       "path": "batched, CUDA graph", "shots_per_launch": q["shots_per_batch"],
+                       "block_x": q["block_x"], "parallelism": "shots" + ("" if world == 1 else " x%d ranks" % world),
+                       "l2": "inputs larger than L2: each step streams %.2f GB of boundary strips and %.2f GB of "
+                             "traces" % (per_rank * sv.nt * (9 * sv.nx + 6 * sv.nz) * 4 / 1e9,
+                                         2 * per_rank * sv.ng * sv.nt * 4 / 1e9)},
+            "gpts_per_s": value * U / 1e9,
+            "hbm_roof_frac_step": (value / world) * B / 1e9 / peak,
+            "algorithmic_gb_per_shot_gradient": B / 1e9,
+            "e2e": {"value": per_rank * world / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+                    "d2h_bytes_per_step": int(d2h)},
+            "clocks": clk,
+            "gpu_launches": int(args.steps * (q["kernels_per_forward"] + q["kernels_per_backward"] + 5))}
+
+    if not args.no_extras:
+        # per-kernel launch durations (CUDA events around every launch)
+        prof = eng.profile_kernels()
+        kb = kernel_bytes_per_shot(sv.nx, sv.nz, sv.npml, sv.ng)
+        shots_launch = q["shots_per_batch"]
+        tot = {k: v["launches"] * v["mean_ms"] for k, v in prof.items()}
+        top = max(tot, key=tot.get)
+        alg = kb[top] * shots_launch
+        achieved = alg / (prof[top]["mean_ms"] / 1000.0) / 1e9
+        traffic = ncu_traffic().get(top)
+        line["roofline"] = {"bound": "hbm", "kernel": top, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                            "frac": achieved / peak, "peak_kind": peak_kind,
+                            "traffic": traffic * shots_launch if traffic else None,
+                            "algorithmic_bytes_per_launch": alg, "mean_launch_ms": prof[top]["mean_ms"],
+                            "kernels": {k: dict(v, share=tot[k] / sum(tot.values())) for k, v in prof.items()}}
+        # plain one-shot-per-launch path on a bounded sample
+        nplain = min(4, per_rank)
+        pe = Engine(sv.nx, sv.nz, sv.npml, sv.nt, sv.dx, sv.dt, src_xz[:nplain], rec_xz[:nplain], path="plain")
+        pe.set_model(sv.vp_init, rho)
+        src_p, obs_p = src_d[:nplain].contiguous(), obs_d[:nplain].contiguous()
+        pe.gradient_l2(src_p, obs_p)
+        torch.cuda.synchronize()
+        ev0.record(stream)
+        pe.gradient_l2(src_p, obs_p)
+        ev1.record(stream)
+        torch.cuda.synchronize()
+        plain = nplain / (ev0.elapsed_time(ev1) / 1000.0)
+        pe.close()
+        line["plain"] = {"value": plain, "unit": UNIT, "sample": "%d shots, one shot per launch, no graph" % nplain}
+        line["batched_over_plain"] = (value / world) / plain
+        if rank == 0 and world == 1:
+            line["cpu_baseline"] = cpu_baseline(sv, rho, src, obs_d.cpu().numpy(), os.cpu_count() or 1)
+    eng.close()
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_mine(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,153 @@
+/*
+ * swit_gb300.h -- C ABI of the GB300 forward/adjoint wave-propagation engine.
+ *
+ * The engine is a drop-in for the computational core behind SWIT's
+ * toolbox/solver.py forward() and adjoint() calls.  In the reference those calls
+ * cross a process boundary (`mpirun fd2dmpi par=<parfile>`, toolbox/solver.py:54
+ * and :79) and exchange files; here the same work is a library call with plain
+ * pointers.  Each entry point below names the reference code it replaces.
+ *
+ * Conventions (identical to the reference's Python side and Fortran files):
+ *   - every 2-D array is z-fastest: model and gradient (nx, nz), i.e. nx records
+ *     of nz floats (toolbox/solver.py:116-119, fd2dmpi/io.f90:590-606);
+ *   - sources (ns, nt); seismograms and adjoint sources (ns, ng_max, nt), one
+ *     trace of nt samples per receiver (fd2dmpi/fdcore.f90:123-128, 181-188;
+ *     toolbox/solver.py:112-113 with fd2dmpi/solver.f90:218);
+ *   - coordinates are in metres, as in coord.txt (toolbox/solver.py:171-180);
+ *     grid indices are npml + int(x/dx) + 1 in single precision
+ *     (fd2dmpi/fdcore.f90:70-72, 124-126).
+ *   - FP32 engines read and write float; FP64 engines (the FP64 build of the
+ *     same kernels, used to state the error of FP32 results) read float inputs
+ *     and write double outputs through the same void* parameters.
+ *
+ * Every call returns 0 on success or a negative SWIT_E_* code; the message of
+ * the last failure on the calling thread is swit_last_error().  Buffers are
+ * owned by the caller; the engine owns its device workspace (wavefields,
+ * boundary strips, seismogram staging).  One engine must not be used from two
+ * threads at once.  `on_device` = 1 means every array argument is a device
+ * pointer and the call is stream-ordered on `stream` (no host synchronisation);
+ * 0 means host arrays, copied inside the call, which returns when the outputs
+ * are written.
+ */
+#ifndef SWIT_GB300_H
+#define SWIT_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SWIT_OK 0
+#define SWIT_E_ARG -1      /* invalid argument (null pointer, bad size)          */
+#define SWIT_E_GEOM -2     /* source/receiver outside the model                  */
+#define SWIT_E_CFL -3      /* dt violates dt < sqrt(3/8) dx / vmax               */
+#define SWIT_E_MODEL -4    /* non-finite or non-positive vp / rho                */
+#define SWIT_E_STATE -5    /* call out of order (e.g. backward before forward)   */
+#define SWIT_E_CUDA -6     /* CUDA runtime error                                 */
+#define SWIT_E_NOMEM -7    /* device allocation failed                           */
+#define SWIT_E_LIMIT -8    /* problem larger than a fixed capacity               */
+
+typedef struct swit_engine swit_engine;
+
+/* Problem description: the parfile keys NX, NZ, NPML, NT_WORK, DX, DT_WORK,
+ * FREESURFACE (fd2dmpi/io.f90:74-96) and the coord.txt geometry
+ * (fd2dmpi/io.f90:126-228). */
+typedef struct swit_desc {
+  int32_t nx, nz, npml, nt;
+  float dx, dt;
+  int32_t free_surface;     /* FREESURFACE, 1 = mirror conditions on           */
+  int32_t ns;               /* number of shots                                  */
+  int32_t ng_max;           /* receivers per shot, maximum                      */
+  const int32_t* ng;        /* [ns] receivers of each shot                       */
+  const float* src_x;       /* [ns]                                              */
+  const float* src_z;       /* [ns]                                              */
+  const float* rec_x;       /* [ns * ng_max]                                     */
+  const float* rec_z;       /* [ns * ng_max]                                     */
+  int32_t precision;        /* 0 = FP32 (default), 1 = FP64 build of the kernels */
+  int32_t path;             /* 0 = batched shots + captured CUDA graph (default),
+                               1 = plain: one shot per launch, one launch per
+                               kernel and step, no graph                          */
+  int32_t shots_per_batch;  /* batched path: shots per launch, 0 = automatic    */
+  int32_t block_x;          /* columns per CTA, 0 = automatic                   */
+} swit_desc;
+
+/* Creates an engine and allocates its device workspace on the current device.
+ * Replaces the setup half of fd2dmpi/solver.f90:36-91 and :120-192
+ * (readparamfile, init_pml, readcoordfile, free_surface) -- the model itself is
+ * given by swit_set_model. */
+int swit_create(const swit_desc* desc, swit_engine** out);
+
+/* Sets vp and rho, (nx, nz) each.  Pads them into the PML by edge replication
+ * (fd2dmpi/io.f90:231-300), finds vmin below the free surface
+ * (fd2dmpi/math.f90:342-361), builds the damping profile
+ * (fd2dmpi/pml.f90:74-101) and the update coefficients of
+ * fd2dmpi/fdcore.f90:79, 99, 312, 339.  Checks the CFL condition of
+ * toolbox/base.py:42, 58-59. */
+int swit_set_model(swit_engine* e, const float* vp, const float* rho, int on_device, void* stream);
+
+/* Forward modeling of every shot: fd2dmpi/fdcore.f90:30-198 driven by
+ * fd2dmpi/solver.f90:93-104 (jobtype=forward_modeling).  src is the already
+ * integrated source (toolbox/solver.py:47), (ns, nt).  seis receives the
+ * pressure seismograms (ns, ng_max, nt); traces beyond ng(is) are zero.
+ * save_boundary = 1 keeps the boundary strips and final wavefields on the
+ * device for swit_backward (STORE_SNAP=1, fdcore.f90:130-177). */
+int swit_forward(swit_engine* e, const float* src, void* seis, int save_boundary, int on_device, void* stream);
+
+/* Reverse-time loop of every shot: wavefield reconstruction from the saved
+ * strips (fd2dmpi/fdcore.f90:202-289), adjoint propagation of the adjoint
+ * sources adj (ns, ng_max, nt) (fdcore.f90:293-375), zero-lag imaging and
+ * illumination (fd2dmpi/solver.f90:230-253), the shot sum and the -2/c scale
+ * (solver.f90:263-270) -- jobtype=adjoint_modeling.  Writes the raw vp kernel
+ * grad, illum_fw and illum_bk, (nx, nz) each: the contents of
+ * src0_kernel_vp.bin, src0_illum_forw.bin, src0_illum_back.bin.  Needs a
+ * preceding swit_forward with save_boundary = 1 on the same model. */
+int swit_backward(swit_engine* e, const float* adj, void* grad, void* illum_fw, void* illum_bk, int on_device,
+                  void* stream);
+
+/* One Waveform-misfit (L2) shot-gradient of every shot in a single call:
+ * forward with strips, the adjoint source syn - obs of every live trace
+ * (toolbox/misfit.py:128-148), the misfit sum_traces sqrt(sum r^2 dt)
+ * (toolbox/misfit.py:263-282), then the reverse loop as swit_backward.  obs is
+ * (ns, ng_max, nt).  seis (optional, may be NULL) receives the synthetics.
+ * misfit (optional) receives one double. */
+int swit_gradient_l2(swit_engine* e, const float* src, const float* obs, void* grad, void* illum_fw,
+                     void* illum_bk, void* seis, double* misfit, int on_device, void* stream);
+
+/* Copies the boundary strips of the last forward run in the reference's
+ * boundary.bin layout, (ns, nt, 9 nx + 6 nz) (fdcore.f90:130-159, 169-170), and
+ * the final interior wavefields p_end, u_end, w_end, (ns, nx, nz) each
+ * (fdcore.f90:162-176).  Any output may be NULL. */
+int swit_export_snapshot(swit_engine* e, void* boundary, void* p_end, void* u_end, void* w_end, int on_device,
+                         void* stream);
+
+/* Profiling hook (the reference has none; fd2dmpi only prints banners,
+ * fd2dmpi/solver.f90:78-84).  Re-runs the forward loop (with strips) and the
+ * reverse loop on the inputs staged by the last swit_gradient_l2 or
+ * swit_forward + swit_backward, launching every stencil kernel directly with a
+ * CUDA event pair around it on `stream`, and returns for each kernel --
+ * [0] forward pressure phase, [1] forward velocity phase, [2] backward velocity
+ * phase, [3] backward pressure phase -- the number of launches and the mean
+ * launch duration in milliseconds.  Synchronises the stream. */
+int swit_profile_kernels(swit_engine* e, int32_t launches[4], double mean_ms[4], void* stream);
+
+/* Sizes the engine has allocated; any pointer may be NULL. */
+int swit_query(const swit_engine* e, int64_t* device_bytes, int32_t* shots_per_batch, int32_t* block_x,
+               int32_t* kernels_per_forward, int32_t* kernels_per_backward);
+
+/* Releases the engine and its device memory. */
+int swit_destroy(swit_engine* e);
+
+/* Message of the last failed call on this thread ("" if none). */
+const char* swit_last_error(void);
+
+/* Host-only helper (no GPU needed): writes the damping profile damp_global
+ * (NZ, NX) that the kernels evaluate in closed form, z-fastest [NX][NZ], for a
+ * given vmin.  Lets tests compare it with fd2dmpi/pml.f90:74-101. */
+int swit_damp_profile(int32_t nx, int32_t nz, int32_t npml, float dx, float vmin, float* out);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SWIT_GB300_H */

@@ -1,0 +1,820 @@
+// engine.cu -- C ABI (include/swit_gb300.h) and device workspace of the GB300
+// forward/adjoint engine.  Kernels are in kernels.cuh.
+//
+// Build: nvcc -gencode arch=compute_103a,code=sm_103a --fmad=false
+//        -Xcompiler -ffp-contract=off (see swit_gb300/build.py).  --fmad=false and
+// the host flag keep every floating-point operation in the reference's order.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/swit_gb300.h"
+#include "kernels.cuh"
+
+using namespace swit;
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  g_err = buf;
+  return code;
+}
+
+#define CK(call)                                                                              \
+  do {                                                                                        \
+    cudaError_t _e = (call);                                                                  \
+    if (_e != cudaSuccess) return fail(SWIT_E_CUDA, "%s: %s (%s:%d)", #call, cudaGetErrorString(_e), __FILE__, __LINE__); \
+  } while (0)
+
+inline int round_up(int a, int m) { return (a + m - 1) / m * m; }
+
+}  // namespace
+
+struct swit_engine {
+  // problem
+  int nx, nz, L, nt, NX, NZ, LD, LDI, fs, fs_flag, ns, ngmax, SL, prec, path;
+  float dx32, dt32;
+  int batch, bx;
+  int device;
+  size_t esz;  // sizeof(R)
+  std::vector<int> ng, isx, isz, risx, risz, colptr, ent_ig, ent_zr;
+  // device tables
+  int *d_ng = nullptr, *d_isx = nullptr, *d_isz = nullptr, *d_risx = nullptr, *d_risz = nullptr;
+  int *d_colptr = nullptr, *d_ig = nullptr, *d_zr = nullptr, *d_live = nullptr;
+  double* d_mtrace = nullptr;
+  // device arrays of type R (float or double)
+  void *A = nullptr, *B = nullptr, *damp = nullptr, *cint = nullptr;
+  void *p = nullptr, *u = nullptr, *w = nullptr, *pb = nullptr, *ub = nullptr, *wb = nullptr;
+  void *pe = nullptr, *ue = nullptr, *we = nullptr, *dg = nullptr, *dfw = nullptr, *dbk = nullptr;
+  void *strips = nullptr, *src = nullptr, *seis_t = nullptr, *adj_t = nullptr;
+  float* d_in = nullptr;     // float staging: sources / obs / adjoint sources from the host
+  void* d_stage = nullptr;   // output staging for host outputs
+  size_t bytes = 0;
+  bool model_set = false, fwd_ready = false;
+  cudaStream_t cap = nullptr;
+  cudaGraphExec_t gfwd[2] = {nullptr, nullptr};
+  cudaGraphExec_t gbwd = nullptr;
+  int launches_fwd = 0, launches_bwd = 0;
+};
+
+namespace {
+
+template <class T>
+int dalloc(swit_engine* e, T** ptr, size_t n) {
+  if (n == 0) n = 1;
+  cudaError_t rc = cudaMalloc((void**)ptr, n * sizeof(T));
+  if (rc != cudaSuccess) {
+    *ptr = nullptr;
+    return fail(SWIT_E_NOMEM, "cudaMalloc of %zu bytes failed: %s", n * sizeof(T), cudaGetErrorString(rc));
+  }
+  e->bytes += n * sizeof(T);
+  return 0;
+}
+
+int valloc(swit_engine* e, void** ptr, size_t n) {
+  if (n == 0) n = 1;
+  cudaError_t rc = cudaMalloc(ptr, n * e->esz);
+  if (rc != cudaSuccess) {
+    *ptr = nullptr;
+    return fail(SWIT_E_NOMEM, "cudaMalloc of %zu bytes failed: %s", n * e->esz, cudaGetErrorString(rc));
+  }
+  e->bytes += n * e->esz;
+  return 0;
+}
+
+void release(swit_engine* e) {
+  for (int i = 0; i < 2; ++i)
+    if (e->gfwd[i]) cudaGraphExecDestroy(e->gfwd[i]);
+  if (e->gbwd) cudaGraphExecDestroy(e->gbwd);
+  if (e->cap) cudaStreamDestroy(e->cap);
+  void* ptrs[] = {e->d_ng, e->d_isx, e->d_isz, e->d_risx, e->d_risz, e->d_colptr, e->d_ig, e->d_zr, e->d_live,
+                  e->d_mtrace, e->A, e->B, e->damp, e->cint, e->p, e->u, e->w, e->pb, e->ub, e->wb, e->pe,
+                  e->ue, e->we, e->dg, e->dfw, e->dbk, e->strips, e->src, e->seis_t, e->adj_t, e->d_in,
+                  e->d_stage};
+  for (void* q : ptrs)
+    if (q) cudaFree(q);
+}
+
+template <class R>
+Grid<R> make_grid(const swit_engine* e) {
+  Grid<R> g;
+  g.nx = e->nx;
+  g.nz = e->nz;
+  g.L = e->L;
+  g.NX = e->NX;
+  g.NZ = e->NZ;
+  g.LD = e->LD;
+  g.LDI = e->LDI;
+  g.fs = e->fs;
+  g.fs_flag = e->fs_flag;
+  g.nt = e->nt;
+  g.ngmax = e->ngmax;
+  g.SL = e->SL;
+  g.FSZ = (size_t)e->NX * e->LD;
+  g.FSI = (size_t)e->nx * e->LDI;
+  g.dt = (R)e->dt32;
+  g.c1 = R(9.0) / R(8.0);    // global.f90:34
+  g.c2 = R(-1.0) / R(24.0);  // global.f90:35
+  g.A = (const R*)e->A;
+  g.B = (const R*)e->B;
+  g.damp = (const R*)e->damp;
+  return g;
+}
+
+inline Receivers make_rec(const swit_engine* e) { return Receivers{e->d_colptr, e->d_ig, e->d_zr}; }
+inline Sources make_src(const swit_engine* e) { return Sources{e->d_isx, e->d_isz, e->d_risx, e->d_risz}; }
+
+// Launch shape of the stencil kernels for a batch of nb shots.
+inline void stencil_shape(const swit_engine* e, int nb, dim3& grid, dim3& block) {
+  block = dim3(32, e->bx, 1);
+  grid = dim3((e->NZ + 31) / 32, (e->NX + e->bx - 1) / e->bx, nb);
+}
+
+// Forward time loop of shots [shot0, shot0+nb): fdcore.f90:75-160.
+template <class R>
+void launch_forward_steps(swit_engine* e, bool store, int shot0, int nb, cudaStream_t st) {
+  Grid<R> g = make_grid<R>(e);
+  dim3 grid, block;
+  stencil_shape(e, nb, grid, block);
+  R* strips = store ? (R*)e->strips : nullptr;
+  for (int it = 2; it <= e->nt; ++it) {
+    k_fwd_p<R><<<grid, block, 0, st>>>(g, make_src(e), (const R*)e->src, (R*)e->p, (const R*)e->u, (const R*)e->w, it,
+                                       shot0);
+    k_fwd_uw<R><<<grid, block, 0, st>>>(g, make_rec(e), (const R*)e->p, (R*)e->u, (R*)e->w, (R*)e->seis_t, strips, it,
+                                        shot0);
+  }
+}
+
+// Reverse time loop of shots [shot0, shot0+nb): solver.f90:230-253.
+template <class R>
+void launch_backward_steps(swit_engine* e, int shot0, int nb, cudaStream_t st) {
+  Grid<R> g = make_grid<R>(e);
+  dim3 grid, block;
+  stencil_shape(e, nb, grid, block);
+  for (int it = e->nt; it >= 2; --it) {
+    k_bwd_uw<R><<<grid, block, 0, st>>>(g, (const R*)e->pb, (R*)e->ub, (R*)e->wb, (const R*)e->pe, (R*)e->ue,
+                                        (R*)e->we, (const R*)e->strips, it, shot0);
+    k_bwd_p<R><<<grid, block, 0, st>>>(g, make_rec(e), make_src(e), (const R*)e->src, (const R*)e->adj_t, (R*)e->pb,
+                                       (const R*)e->ub, (const R*)e->wb, (R*)e->pe, (const R*)e->ue,
+                                       (const R*)e->we, (R*)e->dg, (R*)e->dfw, (R*)e->dbk, (const R*)e->strips, it,
+                                       shot0);
+  }
+}
+
+template <class R>
+int run_forward_loop(swit_engine* e, bool store, cudaStream_t st) {
+  if (e->path == 1) {
+    for (int s = 0; s < e->ns; ++s) launch_forward_steps<R>(e, store, s, 1, st);
+    CK(cudaGetLastError());
+    return 0;
+  }
+  cudaGraphExec_t& ex = e->gfwd[store ? 1 : 0];
+  if (!ex) {
+    cudaGraph_t graph;
+    CK(cudaStreamBeginCapture(e->cap, cudaStreamCaptureModeThreadLocal));
+    for (int s0 = 0; s0 < e->ns; s0 += e->batch) launch_forward_steps<R>(e, store, s0, std::min(e->batch, e->ns - s0), e->cap);
+    cudaError_t rc = cudaStreamEndCapture(e->cap, &graph);
+    if (rc != cudaSuccess) return fail(SWIT_E_CUDA, "forward graph capture: %s", cudaGetErrorString(rc));
+    rc = cudaGraphInstantiate(&ex, graph, 0);
+    cudaGraphDestroy(graph);
+    if (rc != cudaSuccess) {
+      ex = nullptr;
+      return fail(SWIT_E_CUDA, "forward graph instantiate: %s", cudaGetErrorString(rc));
+    }
+  }
+  CK(cudaGraphLaunch(ex, st));
+  return 0;
+}
+
+template <class R>
+int run_backward_loop(swit_engine* e, cudaStream_t st) {
+  if (e->path == 1) {
+    for (int s = 0; s < e->ns; ++s) launch_backward_steps<R>(e, s, 1, st);
+    CK(cudaGetLastError());
+    return 0;
+  }
+  if (!e->gbwd) {
+    cudaGraph_t graph;
+    CK(cudaStreamBeginCapture(e->cap, cudaStreamCaptureModeThreadLocal));
+    for (int s0 = 0; s0 < e->ns; s0 += e->batch) launch_backward_steps<R>(e, s0, std::min(e->batch, e->ns - s0), e->cap);
+    cudaError_t rc = cudaStreamEndCapture(e->cap, &graph);
+    if (rc != cudaSuccess) return fail(SWIT_E_CUDA, "backward graph capture: %s", cudaGetErrorString(rc));
+    rc = cudaGraphInstantiate(&e->gbwd, graph, 0);
+    cudaGraphDestroy(graph);
+    if (rc != cudaSuccess) {
+      e->gbwd = nullptr;
+      return fail(SWIT_E_CUDA, "backward graph instantiate: %s", cudaGetErrorString(rc));
+    }
+  }
+  CK(cudaGraphLaunch(e->gbwd, st));
+  return 0;
+}
+
+template <class R>
+__global__ void k_src_in(const float* __restrict__ in, R* out, int ns, int nt) {
+  const size_t n = (size_t)ns * (nt + 1);
+  for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x) {
+    const int s = (int)(t / (nt + 1)), i = (int)(t - (size_t)s * (nt + 1));
+    out[t] = i < nt ? (R)in[(size_t)s * nt + i] : R(0);  // s(nt+1) = 0
+  }
+}
+
+inline int nblocks(size_t n, int bs = 256) {
+  size_t b = (n + bs - 1) / bs;
+  return (int)std::min<size_t>(b, 152 * 16);
+}
+
+// Copies a float input of n values to device staging (or uses it in place).
+int stage_input(swit_engine* e, const float* in, size_t n, int on_device, cudaStream_t st, const float** out) {
+  if (on_device) {
+    *out = in;
+    return 0;
+  }
+  CK(cudaMemcpyAsync(e->d_in, in, n * sizeof(float), cudaMemcpyHostToDevice, st));
+  *out = e->d_in;
+  return 0;
+}
+
+template <class R>
+int forward_impl(swit_engine* e, const float* src, void* seis, bool store, int on_device, cudaStream_t st) {
+  Grid<R> g = make_grid<R>(e);
+  const float* dsrc;
+  int rc = stage_input(e, src, (size_t)e->ns * e->nt, on_device, st, &dsrc);
+  if (rc) return rc;
+  k_src_in<R><<<nblocks((size_t)e->ns * (e->nt + 1)), 256, 0, st>>>(dsrc, (R*)e->src, e->ns, e->nt);
+  const size_t fb = (size_t)e->ns * g.FSZ * e->esz;
+  CK(cudaMemsetAsync(e->p, 0, fb, st));
+  CK(cudaMemsetAsync(e->u, 0, fb, st));
+  CK(cudaMemsetAsync(e->w, 0, fb, st));
+  rc = run_forward_loop<R>(e, store, st);
+  if (rc) return rc;
+  if (store) {
+    k_copy_end<R><<<nblocks((size_t)e->ns * e->nx * e->nz), 256, 0, st>>>(g, (const R*)e->p, (const R*)e->u,
+                                                                          (const R*)e->w, (R*)e->pe, (R*)e->ue,
+                                                                          (R*)e->we, e->ns);
+  }
+  if (seis) {
+    dim3 grid((e->nt + 31) / 32, (e->ngmax + 31) / 32, e->ns), block(32, 8);
+    void* out = on_device ? seis : e->d_stage;
+    if (e->prec == 0)
+      k_seis_out<R, float><<<grid, block, 0, st>>>((const R*)e->seis_t, (float*)out, e->ns, e->nt, e->ngmax);
+    else
+      k_seis_out<R, double><<<grid, block, 0, st>>>((const R*)e->seis_t, (double*)out, e->ns, e->nt, e->ngmax);
+    if (!on_device)
+      CK(cudaMemcpyAsync(seis, e->d_stage, (size_t)e->ns * e->ngmax * e->nt * e->esz, cudaMemcpyDeviceToHost, st));
+  }
+  CK(cudaGetLastError());
+  e->fwd_ready = store;
+  return 0;
+}
+
+template <class R>
+int backward_core(swit_engine* e, void* grad, void* fw, void* bk, int on_device, cudaStream_t st) {
+  Grid<R> g = make_grid<R>(e);
+  const size_t fb = (size_t)e->ns * g.FSZ * e->esz, ib = (size_t)e->ns * g.FSI * e->esz;
+  CK(cudaMemsetAsync(e->pb, 0, fb, st));
+  CK(cudaMemsetAsync(e->ub, 0, fb, st));
+  CK(cudaMemsetAsync(e->wb, 0, fb, st));
+  CK(cudaMemsetAsync(e->dg, 0, ib, st));
+  CK(cudaMemsetAsync(e->dfw, 0, ib, st));
+  CK(cudaMemsetAsync(e->dbk, 0, ib, st));
+  int rc = run_backward_loop<R>(e, st);
+  if (rc) return rc;
+  const size_t NI = (size_t)e->nx * e->nz;
+  char* stage = (char*)e->d_stage;
+  void* og = on_device ? grad : (grad ? stage : nullptr);
+  void* of = on_device ? fw : (fw ? stage + NI * e->esz : nullptr);
+  void* ob = on_device ? bk : (bk ? stage + 2 * NI * e->esz : nullptr);
+  if (e->prec == 0)
+    k_reduce<R, float><<<nblocks(NI), 256, 0, st>>>(g, (const R*)e->dg, (const R*)e->dfw, (const R*)e->dbk,
+                                                    (const R*)e->cint, e->ns, (float*)og, (float*)of, (float*)ob);
+  else
+    k_reduce<R, double><<<nblocks(NI), 256, 0, st>>>(g, (const R*)e->dg, (const R*)e->dfw, (const R*)e->dbk,
+                                                     (const R*)e->cint, e->ns, (double*)og, (double*)of,
+                                                     (double*)ob);
+  CK(cudaGetLastError());
+  if (!on_device) {
+    if (grad) CK(cudaMemcpyAsync(grad, og, NI * e->esz, cudaMemcpyDeviceToHost, st));
+    if (fw) CK(cudaMemcpyAsync(fw, of, NI * e->esz, cudaMemcpyDeviceToHost, st));
+    if (bk) CK(cudaMemcpyAsync(bk, ob, NI * e->esz, cudaMemcpyDeviceToHost, st));
+  }
+  return 0;
+}
+
+template <class R>
+int backward_impl(swit_engine* e, const float* adj, void* grad, void* fw, void* bk, int on_device, cudaStream_t st) {
+  const float* dadj;
+  int rc = stage_input(e, adj, (size_t)e->ns * e->ngmax * e->nt, on_device, st, &dadj);
+  if (rc) return rc;
+  dim3 grid((e->nt + 31) / 32, (e->ngmax + 31) / 32, e->ns), block(32, 8);
+  k_adj_in<R><<<grid, block, 0, st>>>(dadj, (R*)e->adj_t, e->ns, e->nt, e->ngmax);
+  return backward_core<R>(e, grad, fw, bk, on_device, st);
+}
+
+template <class R>
+int gradient_impl(swit_engine* e, const float* src, const float* obs, void* grad, void* fw, void* bk, void* seis,
+                  double* misfit, int on_device, cudaStream_t st) {
+  // the forward stages the source through d_in; obs needs its own staging
+  int rc = forward_impl<R>(e, src, seis, true, on_device, st);
+  if (rc) return rc;
+  const float* dobs;
+  rc = stage_input(e, obs, (size_t)e->ns * e->ngmax * e->nt, on_device, st, &dobs);
+  if (rc) return rc;
+  k_trace_stats<R><<<dim3(e->ngmax, e->ns), 256, 0, st>>>((const R*)e->seis_t, dobs, e->d_ng, e->nt, e->ngmax,
+                                                          e->dt32, e->d_live, e->d_mtrace);
+  dim3 grid((e->nt + 31) / 32, (e->ngmax + 31) / 32, e->ns), block(32, 8);
+  k_residual<R><<<grid, block, 0, st>>>((const R*)e->seis_t, dobs, e->d_live, (R*)e->adj_t, e->nt, e->ngmax);
+  CK(cudaGetLastError());
+  rc = backward_core<R>(e, grad, fw, bk, on_device, st);
+  if (rc) return rc;
+  if (misfit) {
+    std::vector<double> mt((size_t)e->ns * e->ngmax);
+    CK(cudaMemcpyAsync(mt.data(), e->d_mtrace, mt.size() * sizeof(double), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    double acc = 0.0;
+    for (double v : mt) acc += v;
+    *misfit = acc;
+  }
+  return 0;
+}
+
+// Model setup on the host, in R: padding (io.f90:231-300), vmin
+// (math.f90:342-361), damping table (pml.f90:80-87) and coefficients.
+template <class R>
+int set_model_impl(swit_engine* e, const float* vp, const float* rho, cudaStream_t st) {
+  const int nx = e->nx, nz = e->nz, L = e->L, NX = e->NX, NZ = e->NZ, LD = e->LD;
+  double vmax = 0.0;
+  for (size_t i = 0; i < (size_t)nx * nz; ++i) {
+    if (!std::isfinite(vp[i]) || !(vp[i] > 0.f) || !std::isfinite(rho[i]) || !(rho[i] > 0.f))
+      return fail(SWIT_E_MODEL, "vp/rho must be finite and positive (index %zu: vp=%g rho=%g)", i, vp[i], rho[i]);
+    vmax = std::max(vmax, (double)vp[i]);
+  }
+  // toolbox/base.py:42, 58-59: dt < sqrt(3/8) dx / vmax
+  const double dt_req = std::sqrt(3.0 / 8.0) * (double)e->dx32 / vmax;
+  if (dt_req <= (double)e->dt32)
+    return fail(SWIT_E_CFL, "modeling stability: dt = %.4f ms > dt_required = %.4f ms", e->dt32 * 1000.0,
+                dt_req * 1000.0);
+  std::vector<R> c((size_t)NX * NZ), den((size_t)NX * NZ);
+  auto at = [&](std::vector<R>& m, int iz, int ix) -> R& { return m[(size_t)(ix - 1) * NZ + (iz - 1)]; };
+  auto pad = [&](std::vector<R>& m, const float* in) {
+    for (int ix = 1; ix <= nx; ++ix)
+      for (int iz = 1; iz <= nz; ++iz) at(m, L + iz, L + ix) = (R)in[(size_t)(ix - 1) * nz + (iz - 1)];
+    for (int ix = 1; ix <= L; ++ix)
+      for (int iz = L + 1; iz <= L + nz; ++iz) {
+        at(m, iz, ix) = at(m, iz, L + 1);
+        at(m, iz, NX - L + ix) = at(m, iz, NX - L);
+      }
+    for (int iz = 1; iz <= L; ++iz)
+      for (int ix = 1; ix <= NX; ++ix) {
+        at(m, iz, ix) = at(m, L + 1, ix);
+        at(m, NZ - L + iz, ix) = at(m, NZ - L, ix);
+      }
+  };
+  pad(c, vp);
+  pad(den, rho);
+  // vmin over interior rows i > fs(j) - npml = 1 (flat free surface)
+  R vmin = R(10000000000.0);
+  for (int i = 1; i <= nz; ++i)
+    for (int j = 1; j <= nx; ++j)
+      if (i > e->fs - L && vmin > at(c, L + i, L + j)) vmin = at(c, L + i, L + j);
+  const R dx = (R)e->dx32, dt = (R)e->dt32;
+  std::vector<R> damp(L + 1, R(0));
+  {
+    const R a = (R)(L - 1) * dx;
+    const R kappa = R(3.0) * vmin * (R)std::log(1000.0) / (R(2.0) * a);
+    for (int i = 1; i <= L; ++i) {
+      const R xa = (R)(i - 1) * dx / a;
+      damp[i] = kappa * xa * xa;
+    }
+  }
+  std::vector<R> A((size_t)NX * LD, R(0)), B((size_t)NX * LD, R(0)), ci((size_t)nx * e->LDI, R(1));
+  for (int ix = 1; ix <= NX; ++ix)
+    for (int iz = 1; iz <= NZ; ++iz) {
+      const R dn = at(den, iz, ix), cc = at(c, iz, ix);
+      A[(size_t)(ix - 1) * LD + (iz - 1)] = dn * cc * cc * dt / dx;  // fdcore.f90:79
+      B[(size_t)(ix - 1) * LD + (iz - 1)] = dt / (dn * dx);          // fdcore.f90:99
+    }
+  for (int jx = 1; jx <= nx; ++jx)
+    for (int jz = 1; jz <= nz; ++jz) ci[(size_t)(jx - 1) * e->LDI + (jz - 1)] = at(c, L + jz, L + jx);
+  CK(cudaMemcpyAsync(e->A, A.data(), A.size() * sizeof(R), cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(e->B, B.data(), B.size() * sizeof(R), cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(e->damp, damp.data(), damp.size() * sizeof(R), cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(e->cint, ci.data(), ci.size() * sizeof(R), cudaMemcpyHostToDevice, st));
+  CK(cudaStreamSynchronize(st));  // host vectors go out of scope
+  e->model_set = true;
+  e->fwd_ready = false;
+  return 0;
+}
+
+template <class R>
+int export_impl(swit_engine* e, void* boundary, void* pend, void* uend, void* wend, int on_device, cudaStream_t st) {
+  Grid<R> g = make_grid<R>(e);
+  const size_t NB = (size_t)e->ns * e->nt * e->SL, NI = (size_t)e->ns * e->nx * e->nz;
+  auto one = [&](void* dst, size_t n, auto&& launch) -> int {
+    if (!dst) return 0;
+    void* out = dst;
+    void* tmp = nullptr;
+    if (!on_device) {
+      CK(cudaMallocAsync(&tmp, n * e->esz, st));
+      out = tmp;
+    }
+    launch(out);
+    CK(cudaGetLastError());
+    if (!on_device) {
+      CK(cudaMemcpyAsync(dst, tmp, n * e->esz, cudaMemcpyDeviceToHost, st));
+      CK(cudaFreeAsync(tmp, st));
+    }
+    return 0;
+  };
+  int rc = one(boundary, NB, [&](void* out) {
+    if (e->prec == 0)
+      k_strips_out<R, float><<<nblocks(NB), 256, 0, st>>>(g, (const R*)e->strips, (float*)out, e->ns);
+    else
+      k_strips_out<R, double><<<nblocks(NB), 256, 0, st>>>(g, (const R*)e->strips, (double*)out, e->ns);
+  });
+  if (rc) return rc;
+  void* outs[3] = {pend, uend, wend};
+  void* fields[3] = {e->pe, e->ue, e->we};
+  for (int q = 0; q < 3; ++q) {
+    rc = one(outs[q], NI, [&](void* out) {
+      if (e->prec == 0)
+        k_interior_out<R, float><<<nblocks(NI), 256, 0, st>>>(g, (const R*)fields[q], (float*)out, e->ns);
+      else
+        k_interior_out<R, double><<<nblocks(NI), 256, 0, st>>>(g, (const R*)fields[q], (double*)out, e->ns);
+    });
+    if (rc) return rc;
+  }
+  if (!on_device) CK(cudaStreamSynchronize(st));
+  return 0;
+}
+
+// Per-launch timing of the four stencil kernels with CUDA events.
+template <class R>
+int profile_impl(swit_engine* e, int32_t launches[4], double mean_ms[4], cudaStream_t st) {
+  Grid<R> g = make_grid<R>(e);
+  const int nshot_launch = e->path == 1 ? 1 : e->batch;
+  std::vector<cudaEvent_t> ev[4];
+  auto record = [&](int which) -> cudaEvent_t {
+    cudaEvent_t a;
+    cudaEventCreate(&a);
+    ev[which].push_back(a);
+    cudaEventRecord(a, st);
+    return a;
+  };
+  const size_t fb = (size_t)e->ns * g.FSZ * e->esz, ib = (size_t)e->ns * g.FSI * e->esz;
+  CK(cudaMemsetAsync(e->p, 0, fb, st));
+  CK(cudaMemsetAsync(e->u, 0, fb, st));
+  CK(cudaMemsetAsync(e->w, 0, fb, st));
+  for (int s0 = 0; s0 < e->ns; s0 += nshot_launch) {
+    const int nb = std::min(nshot_launch, e->ns - s0);
+    dim3 grid, block;
+    stencil_shape(e, nb, grid, block);
+    for (int it = 2; it <= e->nt; ++it) {
+      record(0);
+      k_fwd_p<R><<<grid, block, 0, st>>>(g, make_src(e), (const R*)e->src, (R*)e->p, (const R*)e->u,
+                                         (const R*)e->w, it, s0);
+      record(0);
+      record(1);
+      k_fwd_uw<R><<<grid, block, 0, st>>>(g, make_rec(e), (const R*)e->p, (R*)e->u, (R*)e->w, (R*)e->seis_t,
+                                          (R*)e->strips, it, s0);
+      record(1);
+    }
+  }
+  k_copy_end<R><<<nblocks((size_t)e->ns * e->nx * e->nz), 256, 0, st>>>(g, (const R*)e->p, (const R*)e->u,
+                                                                        (const R*)e->w, (R*)e->pe, (R*)e->ue,
+                                                                        (R*)e->we, e->ns);
+  CK(cudaMemsetAsync(e->pb, 0, fb, st));
+  CK(cudaMemsetAsync(e->ub, 0, fb, st));
+  CK(cudaMemsetAsync(e->wb, 0, fb, st));
+  CK(cudaMemsetAsync(e->dg, 0, ib, st));
+  CK(cudaMemsetAsync(e->dfw, 0, ib, st));
+  CK(cudaMemsetAsync(e->dbk, 0, ib, st));
+  for (int s0 = 0; s0 < e->ns; s0 += nshot_launch) {
+    const int nb = std::min(nshot_launch, e->ns - s0);
+    dim3 grid, block;
+    stencil_shape(e, nb, grid, block);
+    for (int it = e->nt; it >= 2; --it) {
+      record(2);
+      k_bwd_uw<R><<<grid, block, 0, st>>>(g, (const R*)e->pb, (R*)e->ub, (R*)e->wb, (const R*)e->pe, (R*)e->ue,
+                                          (R*)e->we, (const R*)e->strips, it, s0);
+      record(2);
+      record(3);
+      k_bwd_p<R><<<grid, block, 0, st>>>(g, make_rec(e), make_src(e), (const R*)e->src, (const R*)e->adj_t,
+                                         (R*)e->pb, (const R*)e->ub, (const R*)e->wb, (R*)e->pe, (const R*)e->ue,
+                                         (const R*)e->we, (R*)e->dg, (R*)e->dfw, (R*)e->dbk, (const R*)e->strips,
+                                         it, s0);
+      record(3);
+    }
+  }
+  CK(cudaGetLastError());
+  CK(cudaStreamSynchronize(st));
+  for (int q = 0; q < 4; ++q) {
+    double tot = 0.0;
+    const size_t n = ev[q].size() / 2;
+    for (size_t i = 0; i < n; ++i) {
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, ev[q][2 * i], ev[q][2 * i + 1]);
+      tot += ms;
+    }
+    for (cudaEvent_t x : ev[q]) cudaEventDestroy(x);
+    launches[q] = (int32_t)n;
+    mean_ms[q] = n ? tot / n : 0.0;
+  }
+  return 0;
+}
+
+// Grid index npml + int(x/dx) + 1 in single precision (fdcore.f90:70, 124).
+inline int gidx(int L, float x, float dx) { return L + (int)(x / dx) + 1; }
+
+}  // namespace
+
+extern "C" {
+
+const char* swit_last_error(void) { return g_err.c_str(); }
+
+int swit_create(const swit_desc* d, swit_engine** out) {
+  if (!d || !out) return fail(SWIT_E_ARG, "null argument");
+  *out = nullptr;
+  if (d->nx < 8 || d->nz < 8) return fail(SWIT_E_ARG, "nx and nz must be >= 8 (got %d, %d)", d->nx, d->nz);
+  if (d->npml < 2) return fail(SWIT_E_ARG, "npml must be >= 2 (got %d)", d->npml);
+  if (d->nt < 2) return fail(SWIT_E_ARG, "nt must be >= 2 (got %d)", d->nt);
+  if (d->ns < 1 || d->ng_max < 1) return fail(SWIT_E_ARG, "ns and ng_max must be >= 1");
+  if (!(d->dx > 0.f) || !(d->dt > 0.f)) return fail(SWIT_E_ARG, "dx and dt must be > 0");
+  if (d->precision != 0 && d->precision != 1) return fail(SWIT_E_ARG, "precision must be 0 or 1");
+  if (d->path != 0 && d->path != 1) return fail(SWIT_E_ARG, "path must be 0 (batched) or 1 (plain)");
+  if (!d->ng || !d->src_x || !d->src_z || !d->rec_x || !d->rec_z) return fail(SWIT_E_ARG, "null geometry array");
+  if (d->ns > 65535) return fail(SWIT_E_LIMIT, "at most 65535 shots per engine");
+
+  swit_engine* e = new swit_engine();
+  e->nx = d->nx;
+  e->nz = d->nz;
+  e->L = d->npml;
+  e->nt = d->nt;
+  e->NX = d->nx + 2 * d->npml;
+  e->NZ = d->nz + 2 * d->npml;
+  e->LD = round_up(e->NZ, 32);
+  e->LDI = round_up(e->nz, 32);
+  e->fs = d->npml + 1;  // io.f90:792, flat topography
+  e->fs_flag = d->free_surface == 1 ? 1 : 0;
+  e->ns = d->ns;
+  e->ngmax = d->ng_max;
+  e->SL = 9 * d->nx + 6 * d->nz;
+  e->prec = d->precision;
+  e->path = d->path;
+  e->dx32 = d->dx;
+  e->dt32 = d->dt;
+  e->esz = e->prec ? sizeof(double) : sizeof(float);
+  e->batch = d->shots_per_batch > 0 ? std::min(d->shots_per_batch, d->ns) : d->ns;
+  e->bx = d->block_x > 0 ? d->block_x : 4;
+  if (32 * e->bx > 256 || (e->bx & (e->bx - 1))) {
+    delete e;
+    return fail(SWIT_E_ARG, "block_x must be a power of two <= 8");
+  }
+  cudaGetDevice(&e->device);
+
+  // geometry: indices exactly as fdcore.f90:70-72, 124-126, 217-218, 349-359
+  const int L = e->L, nx = e->nx, nz = e->nz, NX = e->NX, ns = e->ns, ngm = e->ngmax, fs = e->fs;
+  e->ng.assign(d->ng, d->ng + ns);
+  e->isx.resize(ns);
+  e->isz.resize(ns);
+  e->risx.resize(ns);
+  e->risz.resize(ns);
+  e->colptr.assign((size_t)ns * (NX + 2), 0);
+  e->ent_ig.clear();
+  e->ent_zr.clear();
+  auto inside = [&](float x, int n) { return x >= -0.0f && (int)(x / d->dx) <= n - 1; };
+  for (int s = 0; s < ns; ++s) {
+    if (e->ng[s] < 0 || e->ng[s] > ngm) {
+      delete e;
+      return fail(SWIT_E_ARG, "ng[%d] = %d outside [0, ng_max]", s, d->ng[s]);
+    }
+    const float xs = d->src_x[s], zs = d->src_z[s];
+    if (!inside(xs, nx) || !inside(zs, nz)) {
+      delete e;
+      return fail(SWIT_E_GEOM, "source %d at (%g, %g) m is outside the model", s + 1, xs, zs);
+    }
+    e->isx[s] = gidx(L, xs, d->dx);
+    e->isz[s] = gidx(L, zs, d->dx);
+    if (e->isz[s] == fs) e->isz[s] += 1;
+    // reconstruction-side source subtraction, fdcore.f90:217-218, 250-256
+    const int rx = (int)(xs / d->dx) + 1, rz = (int)(zs / d->dx) + 1;
+    const bool act = rx > 2 && rx < nx - 1 && rz > 3 && rz < nz - 1;
+    e->risx[s] = act ? rx : 0;
+    e->risz[s] = act ? (rz > fs - L ? rz : fs - L + 1) : 0;
+    // receivers grouped by column, in receiver order within a column
+    std::vector<std::pair<int, int>> cols;  // (igx, ig)
+    for (int ig = 0; ig < e->ng[s]; ++ig) {
+      const float xg = d->rec_x[(size_t)s * ngm + ig], zg = d->rec_z[(size_t)s * ngm + ig];
+      if (!inside(xg, nx) || !inside(zg, nz)) {
+        delete e;
+        return fail(SWIT_E_GEOM, "receiver %d of shot %d at (%g, %g) m is outside the model", ig + 1, s + 1, xg, zg);
+      }
+      cols.push_back({gidx(L, xg, d->dx), ig});
+    }
+    std::stable_sort(cols.begin(), cols.end(), [](const auto& a, const auto& b) { return a.first < b.first; });
+    int* cp = &e->colptr[(size_t)s * (NX + 2)];
+    const int base = (int)e->ent_ig.size();
+    std::vector<int> cnt(NX + 2, 0);
+    for (auto& c : cols) {
+      const int ig = c.second;
+      const float zg = d->rec_z[(size_t)s * ngm + ig];
+      int igz = gidx(L, zg, d->dx);
+      // forward gather moves igz == fs down one node (fdcore.f90:126); the
+      // adjoint injects at igz if igz > fs else fs+1 (fdcore.f90:355-359).  For
+      // z >= 0 both give the same row.
+      if (igz == fs) igz += 1;
+      e->ent_ig.push_back(ig);
+      e->ent_zr.push_back(igz);
+      cnt[c.first] += 1;
+    }
+    int acc = base;
+    for (int ix = 0; ix <= NX + 1; ++ix) {
+      cp[ix] = acc;
+      acc += cnt[ix];
+    }
+  }
+  const size_t nent = std::max<size_t>(e->ent_ig.size(), 1);
+  const size_t FSZ = (size_t)e->NX * e->LD, FSI = (size_t)e->nx * e->LDI;
+  int rc = 0;
+#define AL(expr)    \
+  if ((rc = (expr))) { \
+    release(e);      \
+    delete e;        \
+    return rc;       \
+  }
+  AL(dalloc(e, &e->d_ng, ns));
+  AL(dalloc(e, &e->d_isx, ns));
+  AL(dalloc(e, &e->d_isz, ns));
+  AL(dalloc(e, &e->d_risx, ns));
+  AL(dalloc(e, &e->d_risz, ns));
+  AL(dalloc(e, &e->d_colptr, (size_t)ns * (NX + 2)));
+  AL(dalloc(e, &e->d_ig, nent));
+  AL(dalloc(e, &e->d_zr, nent));
+  AL(dalloc(e, &e->d_live, (size_t)ns * ngm));
+  AL(dalloc(e, &e->d_mtrace, (size_t)ns * ngm));
+  AL(valloc(e, &e->A, FSZ));
+  AL(valloc(e, &e->B, FSZ));
+  AL(valloc(e, &e->damp, (size_t)L + 1));
+  AL(valloc(e, &e->cint, FSI));
+  void** fields[] = {&e->p, &e->u, &e->w, &e->pb, &e->ub, &e->wb};
+  for (void** f : fields) AL(valloc(e, f, (size_t)ns * FSZ));
+  void** ifields[] = {&e->pe, &e->ue, &e->we, &e->dg, &e->dfw, &e->dbk};
+  for (void** f : ifields) AL(valloc(e, f, (size_t)ns * FSI));
+  AL(valloc(e, &e->strips, (size_t)ns * e->nt * e->SL));
+  AL(valloc(e, &e->src, (size_t)ns * (e->nt + 1)));
+  AL(valloc(e, &e->seis_t, (size_t)ns * e->nt * ngm));
+  AL(valloc(e, &e->adj_t, (size_t)ns * e->nt * ngm));
+  AL(dalloc(e, &e->d_in, (size_t)ns * ngm * e->nt));
+  AL(valloc(e, &e->d_stage, std::max((size_t)ns * ngm * e->nt, (size_t)3 * nx * nz)));
+#undef AL
+  auto h2d = [&](void* dst, const void* src, size_t bytes) -> int {
+    CK(cudaMemcpy(dst, src, bytes, cudaMemcpyHostToDevice));
+    return 0;
+  };
+  if ((rc = h2d(e->d_ng, e->ng.data(), ns * sizeof(int))) || (rc = h2d(e->d_isx, e->isx.data(), ns * sizeof(int))) ||
+      (rc = h2d(e->d_isz, e->isz.data(), ns * sizeof(int))) ||
+      (rc = h2d(e->d_risx, e->risx.data(), ns * sizeof(int))) ||
+      (rc = h2d(e->d_risz, e->risz.data(), ns * sizeof(int))) ||
+      (rc = h2d(e->d_colptr, e->colptr.data(), e->colptr.size() * sizeof(int))) ||
+      (e->ent_ig.size() && ((rc = h2d(e->d_ig, e->ent_ig.data(), e->ent_ig.size() * sizeof(int))) ||
+                            (rc = h2d(e->d_zr, e->ent_zr.data(), e->ent_zr.size() * sizeof(int)))))) {
+    release(e);
+    delete e;
+    return rc;
+  }
+  // Entries never written by the kernels must read as zero: step 1 of the
+  // seismograms (fdcore.f90 starts at it = 2), traces beyond ng(is), and the
+  // strips of step 1 that the reconstruction inserts at it = 2.
+  cudaError_t ce = cudaMemset(e->seis_t, 0, (size_t)ns * e->nt * ngm * e->esz);
+  if (ce == cudaSuccess) ce = cudaMemset(e->strips, 0, (size_t)ns * e->nt * e->SL * e->esz);
+  if (ce == cudaSuccess) ce = cudaMemset(e->adj_t, 0, (size_t)ns * e->nt * ngm * e->esz);
+  if (ce == cudaSuccess) ce = cudaStreamCreateWithFlags(&e->cap, cudaStreamNonBlocking);
+  if (ce != cudaSuccess) {
+    rc = fail(SWIT_E_CUDA, "engine initialisation: %s", cudaGetErrorString(ce));
+    release(e);
+    delete e;
+    return rc;
+  }
+  const int waves = (ns + e->batch - 1) / e->batch;
+  const int per = e->path == 1 ? ns : waves;
+  e->launches_fwd = per * (e->nt - 1) * 2;
+  e->launches_bwd = per * (e->nt - 1) * 2;
+  *out = e;
+  return 0;
+}
+
+int swit_set_model(swit_engine* e, const float* vp, const float* rho, int on_device, void* stream) {
+  if (!e || !vp || !rho) return fail(SWIT_E_ARG, "null argument");
+  cudaStream_t st = (cudaStream_t)stream;
+  const size_t n = (size_t)e->nx * e->nz;
+  std::vector<float> hv, hr;
+  if (on_device) {
+    hv.resize(n);
+    hr.resize(n);
+    CK(cudaMemcpyAsync(hv.data(), vp, n * sizeof(float), cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(hr.data(), rho, n * sizeof(float), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    vp = hv.data();
+    rho = hr.data();
+  }
+  return e->prec ? set_model_impl<double>(e, vp, rho, st) : set_model_impl<float>(e, vp, rho, st);
+}
+
+int swit_forward(swit_engine* e, const float* src, void* seis, int save_boundary, int on_device, void* stream) {
+  if (!e || !src) return fail(SWIT_E_ARG, "null argument");
+  if (!e->model_set) return fail(SWIT_E_STATE, "swit_set_model must be called before swit_forward");
+  cudaStream_t st = (cudaStream_t)stream;
+  int rc = e->prec ? forward_impl<double>(e, src, seis, save_boundary != 0, on_device, st)
+                   : forward_impl<float>(e, src, seis, save_boundary != 0, on_device, st);
+  if (rc) return rc;
+  if (!on_device) CK(cudaStreamSynchronize(st));
+  return 0;
+}
+
+int swit_backward(swit_engine* e, const float* adj, void* grad, void* illum_fw, void* illum_bk, int on_device,
+                  void* stream) {
+  if (!e || !adj) return fail(SWIT_E_ARG, "null argument");
+  if (!e->fwd_ready) return fail(SWIT_E_STATE, "swit_backward needs a preceding swit_forward with save_boundary=1");
+  cudaStream_t st = (cudaStream_t)stream;
+  int rc = e->prec ? backward_impl<double>(e, adj, grad, illum_fw, illum_bk, on_device, st)
+                   : backward_impl<float>(e, adj, grad, illum_fw, illum_bk, on_device, st);
+  if (rc) return rc;
+  if (!on_device) CK(cudaStreamSynchronize(st));
+  return 0;
+}
+
+int swit_gradient_l2(swit_engine* e, const float* src, const float* obs, void* grad, void* illum_fw, void* illum_bk,
+                     void* seis, double* misfit, int on_device, void* stream) {
+  if (!e || !src || !obs) return fail(SWIT_E_ARG, "null argument");
+  if (!e->model_set) return fail(SWIT_E_STATE, "swit_set_model must be called before swit_gradient_l2");
+  cudaStream_t st = (cudaStream_t)stream;
+  int rc = e->prec ? gradient_impl<double>(e, src, obs, grad, illum_fw, illum_bk, seis, misfit, on_device, st)
+                   : gradient_impl<float>(e, src, obs, grad, illum_fw, illum_bk, seis, misfit, on_device, st);
+  if (rc) return rc;
+  if (!on_device) CK(cudaStreamSynchronize(st));
+  return 0;
+}
+
+int swit_export_snapshot(swit_engine* e, void* boundary, void* p_end, void* u_end, void* w_end, int on_device,
+                         void* stream) {
+  if (!e) return fail(SWIT_E_ARG, "null argument");
+  if (!e->fwd_ready) return fail(SWIT_E_STATE, "no saved forward run (swit_forward with save_boundary=1)");
+  cudaStream_t st = (cudaStream_t)stream;
+  return e->prec ? export_impl<double>(e, boundary, p_end, u_end, w_end, on_device, st)
+                 : export_impl<float>(e, boundary, p_end, u_end, w_end, on_device, st);
+}
+
+int swit_profile_kernels(swit_engine* e, int32_t launches[4], double mean_ms[4], void* stream) {
+  if (!e || !launches || !mean_ms) return fail(SWIT_E_ARG, "null argument");
+  if (!e->model_set) return fail(SWIT_E_STATE, "swit_set_model must be called first");
+  cudaStream_t st = (cudaStream_t)stream;
+  return e->prec ? profile_impl<double>(e, launches, mean_ms, st) : profile_impl<float>(e, launches, mean_ms, st);
+}
+
+int swit_query(const swit_engine* e, int64_t* device_bytes, int32_t* shots_per_batch, int32_t* block_x,
+               int32_t* kernels_per_forward, int32_t* kernels_per_backward) {
+  if (!e) return fail(SWIT_E_ARG, "null argument");
+  if (device_bytes) *device_bytes = (int64_t)e->bytes;
+  if (shots_per_batch) *shots_per_batch = e->path == 1 ? 1 : e->batch;
+  if (block_x) *block_x = e->bx;
+  if (kernels_per_forward) *kernels_per_forward = e->launches_fwd;
+  if (kernels_per_backward) *kernels_per_backward = e->launches_bwd;
+  return 0;
+}
+
+int swit_destroy(swit_engine* e) {
+  if (!e) return 0;
+  release(e);
+  delete e;
+  return 0;
+}
+
+int swit_damp_profile(int32_t nx, int32_t nz, int32_t npml, float dx, float vmin, float* out) {
+  if (nx < 1 || nz < 1 || npml < 2 || !(dx > 0.f) || !out) return fail(SWIT_E_ARG, "bad argument");
+  const int NX = nx + 2 * npml, NZ = nz + 2 * npml, L = npml;
+  std::vector<float> damp(L + 1, 0.f);
+  const float a = (float)(L - 1) * dx;
+  const float kappa = 3.0f * vmin * (float)std::log(1000.0) / (2.0f * a);
+  for (int i = 1; i <= L; ++i) {
+    const float xa = (float)(i - 1) * dx / a;
+    damp[i] = kappa * xa * xa;
+  }
+  for (int ix = 1; ix <= NX; ++ix)
+    for (int iz = 1; iz <= NZ; ++iz) out[(size_t)(ix - 1) * NZ + (iz - 1)] = damp_at(damp.data(), iz, ix, L, NX, NZ);
+  return 0;
+}
+
+}  // extern "C"

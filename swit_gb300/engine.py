@@ -1,0 +1,204 @@
+"""Python front end of the GB300 engine (one object per model geometry).
+
+``Engine`` owns a ``swit_engine`` from the C ABI (include/swit_gb300.h).  Arrays
+may be numpy arrays (host buffers, copied inside the call) or CUDA torch
+tensors (device buffers; the call is ordered on torch's current stream).
+Layouts follow SWIT's Python side: model and gradients (nx, nz), sources
+(ns, nt), seismograms and adjoint sources (ns, ng_max, nt).
+"""
+import ctypes as C
+
+import numpy as np
+
+from . import _lib
+
+
+def _is_torch(a):
+    return type(a).__module__.split(".")[0] == "torch"
+
+
+class Engine:
+    """Batched forward / adjoint / imaging engine for one model geometry.
+
+    Parameters mirror the fd2dmpi parfile (NX, NZ, DX, NPML, NT_WORK, DT_WORK,
+    FREESURFACE; fd2dmpi/io.f90:74-96) and coord.txt (toolbox/solver.py:171-180).
+    ``src_xz`` is (ns, 2) and ``rec_xz`` is (ns, ng_max, 2) or (ng, 2) shared by
+    all shots, in metres.
+    """
+
+    def __init__(self, nx, nz, npml, nt, dx, dt, src_xz, rec_xz, free_surface=1, ng=None, precision="fp32",
+                 path="batched", shots_per_batch=0, block_x=0):
+        lib = _lib.load()
+        src_xz = np.asarray(src_xz, dtype=np.float32).reshape(-1, 2)
+        rec_xz = np.asarray(rec_xz, dtype=np.float32)
+        if rec_xz.ndim == 2:
+            rec_xz = np.broadcast_to(rec_xz, (src_xz.shape[0],) + rec_xz.shape)
+        if rec_xz.ndim != 3 or rec_xz.shape[0] != src_xz.shape[0] or rec_xz.shape[2] != 2:
+            raise ValueError("rec_xz must be (ns, ng_max, 2) or (ng, 2)")
+        self.nx, self.nz, self.npml, self.nt = int(nx), int(nz), int(npml), int(nt)
+        self.dx, self.dt = float(np.float32(dx)), float(np.float32(dt))
+        self.ns, self.ngmax = src_xz.shape[0], rec_xz.shape[1]
+        self.precision = precision
+        self.fp64 = precision == "fp64"
+        if precision not in ("fp32", "fp64"):
+            raise ValueError("precision must be 'fp32' or 'fp64'")
+        if path not in ("batched", "plain"):
+            raise ValueError("path must be 'batched' or 'plain'")
+        self.path = path
+        self._keep = dict(
+            ng=np.ascontiguousarray(np.full(self.ns, self.ngmax) if ng is None else ng, dtype=np.int32),
+            xs=np.ascontiguousarray(src_xz[:, 0]), zs=np.ascontiguousarray(src_xz[:, 1]),
+            xg=np.ascontiguousarray(rec_xz[:, :, 0]).reshape(-1), zg=np.ascontiguousarray(rec_xz[:, :, 1]).reshape(-1))
+        k = self._keep
+        d = _lib.SwitDesc(self.nx, self.nz, self.npml, self.nt, self.dx, self.dt, int(free_surface), self.ns,
+                          self.ngmax, k["ng"].ctypes.data, k["xs"].ctypes.data, k["zs"].ctypes.data,
+                          k["xg"].ctypes.data, k["zg"].ctypes.data, 1 if self.fp64 else 0,
+                          1 if path == "plain" else 0, int(shots_per_batch), int(block_x))
+        h = C.c_void_p()
+        _lib.check(lib.swit_create(C.byref(d), C.byref(h)))
+        self._h = h
+        self._lib = lib
+
+    # ------------------------------------------------------------------ utils
+    @property
+    def out_dtype(self):
+        return np.float64 if self.fp64 else np.float32
+
+    def _ptr(self, a, dtype):
+        """Returns (pointer, on_device) for a numpy array or CUDA tensor input."""
+        if a is None:
+            return None, None
+        if _is_torch(a):
+            import torch
+            if not a.is_cuda:
+                a = a.detach().numpy()
+            else:
+                want = torch.float32 if dtype == np.float32 else torch.float64
+                if a.dtype != want or not a.is_contiguous():
+                    raise ValueError("device arrays must be contiguous %s" % want)
+                return a.data_ptr(), 1
+        if not isinstance(a, np.ndarray) or a.dtype != dtype or not a.flags.c_contiguous:
+            raise ValueError("host arrays must be C-contiguous %s" % np.dtype(dtype).name)
+        return a.ctypes.data, 0
+
+    @staticmethod
+    def _stream(on_device):
+        if on_device:
+            import torch
+            return torch.cuda.current_stream().cuda_stream
+        return None
+
+    def _new(self, shape, like_device):
+        if like_device:
+            import torch
+            return torch.zeros(shape, dtype=torch.float64 if self.fp64 else torch.float32, device="cuda")
+        return np.zeros(shape, self.out_dtype)
+
+    @staticmethod
+    def _f32(a):
+        if _is_torch(a):
+            return a.contiguous().float() if a.is_cuda else a.detach().cpu().numpy().astype(np.float32)
+        return np.ascontiguousarray(a, dtype=np.float32)
+
+    # ------------------------------------------------------------------ API
+    def set_model(self, vp, rho):
+        """vp, rho: (nx, nz) float32."""
+        vp, rho = self._f32(vp), self._f32(rho)
+        if tuple(vp.shape) != (self.nx, self.nz) or tuple(rho.shape) != (self.nx, self.nz):
+            raise ValueError("vp/rho must be (nx, nz) = (%d, %d)" % (self.nx, self.nz))
+        pv, dev = self._ptr(vp, np.float32)
+        pr, dev2 = self._ptr(rho, np.float32)
+        if dev != dev2:
+            raise ValueError("vp and rho must both be host or both be device arrays")
+        _lib.check(self._lib.swit_set_model(self._h, pv, pr, dev, self._stream(dev)))
+
+    def forward(self, src, save_boundary=True, seis=None):
+        """Seismograms (ns, ng_max, nt) of source functions src (ns, nt)."""
+        src = self._f32(src)
+        if tuple(src.shape) != (self.ns, self.nt):
+            raise ValueError("src must be (ns, nt) = (%d, %d)" % (self.ns, self.nt))
+        ps, dev = self._ptr(src, np.float32)
+        if seis is None:
+            seis = self._new((self.ns, self.ngmax, self.nt), dev)
+        po, _ = self._ptr(seis, self.out_dtype)
+        _lib.check(self._lib.swit_forward(self._h, ps, po, 1 if save_boundary else 0, dev, self._stream(dev)))
+        return seis
+
+    def backward(self, adj, grad=None, illum_fw=None, illum_bk=None):
+        """(grad, illum_fw, illum_bk), each (nx, nz), for adjoint sources adj (ns, ng_max, nt)."""
+        adj = self._f32(adj)
+        if tuple(adj.shape) != (self.ns, self.ngmax, self.nt):
+            raise ValueError("adj must be (ns, ng_max, nt)")
+        pa, dev = self._ptr(adj, np.float32)
+        outs = [x if x is not None else self._new((self.nx, self.nz), dev) for x in (grad, illum_fw, illum_bk)]
+        ptrs = [self._ptr(x, self.out_dtype)[0] for x in outs]
+        _lib.check(self._lib.swit_backward(self._h, pa, ptrs[0], ptrs[1], ptrs[2], dev, self._stream(dev)))
+        return tuple(outs)
+
+    def gradient_l2(self, src, obs, return_seis=False):
+        """Waveform-misfit gradient: returns dict(grad, illum_fw, illum_bk, misfit[, seis])."""
+        src, obs = self._f32(src), self._f32(obs)
+        ps, dev = self._ptr(src, np.float32)
+        po, dev2 = self._ptr(obs, np.float32)
+        if dev != dev2:
+            raise ValueError("src and obs must both be host or both be device arrays")
+        outs = [self._new((self.nx, self.nz), dev) for _ in range(3)]
+        seis = self._new((self.ns, self.ngmax, self.nt), dev) if return_seis else None
+        m = C.c_double(0.0)
+        _lib.check(self._lib.swit_gradient_l2(self._h, ps, po, *[self._ptr(x, self.out_dtype)[0] for x in outs],
+                                              self._ptr(seis, self.out_dtype)[0], C.byref(m), dev,
+                                              self._stream(dev)))
+        out = dict(grad=outs[0], illum_fw=outs[1], illum_bk=outs[2], misfit=m.value)
+        if return_seis:
+            out["seis"] = seis
+        return out
+
+    def export_snapshot(self):
+        """Boundary strips (ns, nt, 9nx+6nz) and p_end/u_end/w_end (ns, nx, nz) of the last saved forward."""
+        b = np.zeros((self.ns, self.nt, 9 * self.nx + 6 * self.nz), self.out_dtype)
+        ends = [np.zeros((self.ns, self.nx, self.nz), self.out_dtype) for _ in range(3)]
+        _lib.check(self._lib.swit_export_snapshot(self._h, b.ctypes.data, *[x.ctypes.data for x in ends], 0, None))
+        return dict(boundary=b, p_end=ends[0], u_end=ends[1], w_end=ends[2])
+
+    def profile_kernels(self):
+        """Mean launch duration (ms) and launch count of the four stencil kernels,
+        timed with CUDA events on torch's current stream (see swit_profile_kernels)."""
+        import torch
+        n = (C.c_int32 * 4)()
+        ms = (C.c_double * 4)()
+        _lib.check(self._lib.swit_profile_kernels(self._h, n, ms, torch.cuda.current_stream().cuda_stream))
+        names = ("fwd_p", "fwd_uw", "bwd_uw", "bwd_p")
+        return {k: dict(launches=int(n[i]), mean_ms=float(ms[i])) for i, k in enumerate(names)}
+
+    def query(self):
+        by = C.c_int64()
+        sb, bx, kf, kb = C.c_int32(), C.c_int32(), C.c_int32(), C.c_int32()
+        _lib.check(self._lib.swit_query(self._h, C.byref(by), C.byref(sb), C.byref(bx), C.byref(kf), C.byref(kb)))
+        return dict(device_bytes=by.value, shots_per_batch=sb.value, block_x=bx.value, kernels_per_forward=kf.value,
+                    kernels_per_backward=kb.value)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.swit_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+
+def damp_profile(nx, nz, npml, dx, vmin):
+    """Closed-form damping profile damp_global (NX, NZ) the kernels evaluate (host-side, no GPU)."""
+    lib = _lib.load()
+    out = np.zeros((nx + 2 * npml, nz + 2 * npml), np.float32)
+    _lib.check(lib.swit_damp_profile(int(nx), int(nz), int(npml), float(np.float32(dx)), float(np.float32(vmin)),
+                                     out.ctypes.data))
+    return out

@@ -1,0 +1,88 @@
+"""CPU tests of the C-ABI library: it loads, exports every declared symbol,
+validates its arguments before touching the GPU, and evaluates the reference's
+damping profile in closed form."""
+import ctypes as C
+import os
+import re
+
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from swit_gb300 import _lib, build, damp_profile, survey
+
+HEADER = os.path.join(os.path.dirname(build.HERE), "include", "swit_gb300.h")
+
+
+def declared_symbols():
+    txt = open(HEADER).read()
+    txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+    return sorted(set(re.findall(r"\b(swit_[a-z0-9_]+)\s*\(", txt)))
+
+
+def test_library_builds_and_exports_every_declared_symbol():
+    lib = _lib.load()
+    names = declared_symbols()
+    assert set(names) == set(_lib.EXPORTS), names
+    for n in names:
+        assert hasattr(lib, n), n
+
+
+def _desc(s, **over):
+    ng = np.full(s.ns, s.ng, np.int32)
+    xs = np.ascontiguousarray(s.src_xz[:, 0])
+    zs = np.ascontiguousarray(s.src_xz[:, 1])
+    xg = np.ascontiguousarray(s.rec_xz[:, :, 0]).reshape(-1)
+    zg = np.ascontiguousarray(s.rec_xz[:, :, 1]).reshape(-1)
+    keep = [ng, xs, zs, xg, zg]
+    f = dict(nx=s.nx, nz=s.nz, npml=s.npml, nt=s.nt, dx=s.dx, dt=s.dt, free_surface=1, ns=s.ns, ng_max=s.ng,
+             ng=ng.ctypes.data, src_x=xs.ctypes.data, src_z=zs.ctypes.data, rec_x=xg.ctypes.data,
+             rec_z=zg.ctypes.data, precision=0, path=0, shots_per_batch=0, block_x=0)
+    f.update(over)
+    return _lib.SwitDesc(**f), keep
+
+
+@pytest.mark.parametrize("over,code", [
+    (dict(nx=4), _lib.SwitError), (dict(npml=1), _lib.SwitError), (dict(nt=1), _lib.SwitError),
+    (dict(dx=0.0), _lib.SwitError), (dict(precision=3), _lib.SwitError), (dict(block_x=3), _lib.SwitError),
+])
+def test_create_rejects_bad_descriptions_before_any_gpu_work(over, code):
+    lib = _lib.load()
+    s = survey.small()
+    d, keep = _desc(s, **over)
+    h = C.c_void_p()
+    rc = lib.swit_create(C.byref(d), C.byref(h))
+    assert rc == -1
+    assert lib.swit_last_error().decode()
+
+
+def test_create_rejects_receivers_outside_the_model():
+    lib = _lib.load()
+    s = survey.small()
+    s.rec_xz = s.rec_xz.copy()
+    s.rec_xz[1, 3, 0] = (s.nx + 5) * s.dx
+    d, keep = _desc(s)
+    h = C.c_void_p()
+    assert lib.swit_create(C.byref(d), C.byref(h)) == -2
+    assert "receiver 4 of shot 2" in lib.swit_last_error().decode()
+
+
+def test_null_arguments_are_errors():
+    lib = _lib.load()
+    h = C.c_void_p()
+    assert lib.swit_create(None, C.byref(h)) == -1
+    assert lib.swit_set_model(None, None, None, 0, None) == -1
+    assert lib.swit_forward(None, None, None, 1, 0, None) == -1
+    assert lib.swit_destroy(None) == 0
+
+
+@pytest.mark.parametrize("nx,nz,npml", [(48, 32, 10), (30, 17, 7), (201, 101, 40)])
+def test_closed_form_damping_equals_reference_loops(nx, nz, npml):
+    s = survey.small(nx=nx, nz=nz, npml=npml)
+    vp = s.vp_true
+    pb = O.Problem(nx, nz, npml, 10, s.dx, s.dt, s.src_xz, s.rec_xz)
+    ref = O.damp_profile(pb, vp, s.rho(vp))
+    # vmin below the free surface: rows 2..nz of the interior (math.f90:342-361)
+    vmin = np.float32(vp[:, 1:].min())
+    mine = damp_profile(nx, nz, npml, s.dx, vmin)
+    np.testing.assert_array_equal(mine, ref)
