@@ -1,0 +1,48 @@
+"""torch.autograd wrapper: seismograms = F(vp) with the engine's reverse loop as
+the backward, so misfits written in torch get their adjoint sources from autograd.
+
+    seis = propagate(engine, vp, rho, src)      # (ns, ng_max, nt), CUDA tensor
+    loss = misfit(seis, obs); loss.backward()   # vp.grad filled by the engine
+
+Backward feeds dL/dseis to the reverse loop as the adjoint source (what
+toolbox/solver.py:72-75 writes to parfile/adjoint_source) and returns the
+reference's vp kernel g = -2/c sum_t p_f (p_b(t+1) - p_b(t))
+(fd2dmpi/solver.f90:237, 270) divided by dt.  The reference's adjoint injects
+dt * r (fdcore.f90:351-356), so g/dt approximates dL/dvp; it is the
+continuous-adjoint imaging gradient of fd2dmpi, not the exact transpose of the
+discrete forward map (the central finite-difference agreement is measured by
+tests/test_gpu_autograd.py).
+
+If the engine ran another forward between this forward and its backward, the
+boundary strips are recomputed first (checkpointed recomputation).
+"""
+import torch
+
+
+class _Propagate(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, vp, rho, src, engine):
+        engine.set_model(vp.detach().contiguous().float(), rho.detach().contiguous().float())
+        seis = engine.forward(src.detach().contiguous().float(), save_boundary=True)
+        engine._generation = getattr(engine, "_generation", 0) + 1
+        ctx.engine = engine
+        ctx.generation = engine._generation
+        ctx.save_for_backward(vp, rho, src)
+        return seis
+
+    @staticmethod
+    def backward(ctx, grad_seis):
+        engine = ctx.engine
+        vp, rho, src = ctx.saved_tensors
+        if engine._generation != ctx.generation:
+            engine.set_model(vp.detach().contiguous().float(), rho.detach().contiguous().float())
+            engine.forward(src.detach().contiguous().float(), save_boundary=True)
+            engine._generation += 1
+        g, _, _ = engine.backward(grad_seis.detach().contiguous().float())
+        g = g / engine.dt
+        return g.to(vp.dtype), None, None, None
+
+
+def propagate(engine, vp, rho, src):
+    """Differentiable forward modeling of every shot (gradient w.r.t. vp only)."""
+    return _Propagate.apply(vp, rho, src, engine)

@@ -1,0 +1,52 @@
+"""CPU tests of the host-side file contract: SU header layout and values,
+parfile and coord.txt formats."""
+import numpy as np
+
+from swit_gb300 import suio
+
+
+def test_su_header_is_240_bytes_with_the_documented_byte_positions(tmp_path):
+    # byte positions documented in fd2dmpi/su.f90 (1-based, SEG-Y/SU convention)
+    pos = {"tracl": 1, "cdp": 21, "offset": 37, "sx": 73, "gx": 81, "ns": 115, "dt": 117, "d1": 181, "d2": 189,
+           "f2": 193, "mark": 205, "unass": 207}
+    for k, p in pos.items():
+        assert suio._HDR.fields[k][1] == p - 1, k
+    tr = np.arange(3 * 7, dtype=np.float32).reshape(3, 7)
+    path = tmp_path / "s.su"
+    suio.write_su(str(path), tr, 0.002, 1000.0, np.array([0.0, 25.0, 1012.5], np.float32))
+    raw = path.read_bytes()
+    assert len(raw) == 3 * (240 + 7 * 4)
+    h, d = suio.read_su(str(path))
+    np.testing.assert_array_equal(d, tr)
+    assert list(h["tracl"]) == [1, 2, 3] and list(h["tracr"]) == [1, 2, 3]
+    assert set(h["ns"]) == {7} and set(h["dt"]) == {2000} and set(h["fldr"]) == {1} and set(h["ep"]) == {1}
+    assert list(h["gx"]) == [0, 25, 1013]           # NINT rounds half away from zero
+    assert list(h["sx"]) == [1000] * 3
+    assert list(h["offset"]) == [-1000, -975, 13]
+    assert list(h["cdp"]) == [500, 513, 1006]       # nint(0.5 (xs + xg)) in single precision
+    assert list(h["cdpt"]) == list(h["cdp"])
+    assert np.allclose(h["d1"], 0.002) and set(h["d2"]) == {1.0} and set(h["f1"]) == {0.0}
+    assert not np.any(h["unass"]) and not np.any(h["trid"])
+
+
+def test_su_dt_is_truncated_in_single_precision():
+    for dt, us in ((0.002, 2000), (0.001, 1000), (0.0015, 1500), (0.0005, 500)):
+        h = suio.su_headers(10, dt, 0.0, np.zeros(1, np.float32))
+        assert h["dt"][0] == us
+
+
+def test_parfile_and_coord_formats(tmp_path):
+    p = tmp_path / "parfile"
+    suio.write_parfile(str(p), "forward_modeling", "/w/", "syn", 481, 141, 25.0, 40, 4000, 0.002, True, 1, 1)
+    kv = suio.read_parfile(str(p))
+    assert kv["jobtype"] == "forward_modeling" and kv["DATA_OUT"] == "/w/data/syn/src"
+    assert kv["DX"] == "25.000000" and kv["DT_WORK"] == "0.002000" and kv["FREESURFACE"] == "1"
+    assert kv["NX"] == "481" and kv["NPML"] == "40" and kv["STORE_SNAP"] == "1"
+    c = tmp_path / "coord.txt"
+    src = np.array([[0.0, 25.0], [12.34, 25.0]])
+    rec = np.array([[[0.0, 25.0], [25.0, 25.0]], [[0.0, 25.0], [25.0, 25.0]]])
+    suio.write_coord(str(c), src, rec)
+    lines = c.read_text().splitlines()
+    assert lines[0] == "     1      1        0.0       25.0        0.0       25.0        1.0"
+    assert lines[2].split()[2] == "12.3"
+    assert suio.parfile_value("%10.1f", 12.34) == np.float32(12.3)
