@@ -205,7 +205,7 @@ def run_mine(args):
     import torch
     import torch.distributed as dist
 
-    from swit_gb300 import Engine, survey
+    from swit_gb300 import Engine, shots, survey
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -215,8 +215,8 @@ def run_mine(args):
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
     per_rank = args.shots or 49
     full = survey.config(1, ns=per_rank * world, nt=args.nt)
-    # rank r owns a contiguous block of shots (fd2dmpi/mmi_mpi.f90:52-80 with equal blocks)
-    lo, hi = rank * per_rank, (rank + 1) * per_rank
+    # rank r owns a contiguous block of shots (fd2dmpi/mmi_mpi.f90:52-80)
+    lo, hi = shots.assigned(per_rank * world, rank, world)
     sv = full
     src_xz, rec_xz = full.src_xz[lo:hi], full.rec_xz[lo:hi]
     rho = sv.rho(sv.vp_true)
@@ -233,9 +233,7 @@ def run_mine(args):
 
     def step_device():
         out = eng.gradient_l2(src_d, obs_d)
-        if world > 1:
-            for k in ("grad", "illum_fw", "illum_bk"):
-                dist.all_reduce(out[k])
+        shots.allreduce_sum([out["grad"], out["illum_fw"], out["illum_bk"]])
         return out
 
     for _ in range(args.warmup):
@@ -275,7 +273,7 @@ def run_mine(args):
         out = eng.gradient_l2(src_h, obs_h)
         if world > 1:
             g = torch.from_numpy(np.stack([out["grad"], out["illum_fw"], out["illum_bk"]])).cuda()
-            dist.all_reduce(g)
+            shots.allreduce_sum([g])
             g.cpu()
         return out
 
