@@ -43,6 +43,8 @@ def parse():
     ap.add_argument("--nt", type=int, default=None, help="time steps (default 4000)")
     ap.add_argument("--batch", type=int, default=0, help="shots per launch (0 = engine default)")
     ap.add_argument("--block-x", type=int, default=0)
+    ap.add_argument("--kernel", default="auto", choices=["auto", "fused", "split"])
+    ap.add_argument("--no-tune", action="store_true", help="skip the launch-configuration autotuner")
     ap.add_argument("--no-extras", action="store_true", help="skip plain path, CPU baseline and kernel profile")
     return ap.parse_args()
 
@@ -75,6 +77,10 @@ def kernel_bytes_per_shot(nx, nz, npml, ng):
         "fwd_uw": 24 * npts + 4 * (9 * nx + 6 * nz) + 4 * ng,  # u, w r/w, p, B; strips, trace samples
         "bwd_uw": 24 * npts + 24 * nint + 4 * (nx + 2 * nz),   # adjoint u, w; reconstruction u, w; strips
         "bwd_p": 20 * npts + 44 * nint + 4 * (5 * nx + 4 * nz) + 4 * ng,  # adjoint p; reco p; imaging; strips
+        # fused: p, u, w, A, B read and p, u, w written once; the interior adds the
+        # reconstruction state and the three imaging sums
+        "fwd_step": 32 * npts + 4 * (9 * nx + 6 * nz) + 4 * ng,
+        "bwd_step": 32 * npts + 48 * nint + 4 * (6 * nx + 6 * nz) + 4 * ng,
     }
 
 
@@ -221,8 +227,15 @@ def run_mine(args):
     src_xz, rec_xz = full.src_xz[lo:hi], full.rec_xz[lo:hi]
     rho = sv.rho(sv.vp_true)
     src = sv.source()[lo:hi].copy()
-    eng = Engine(sv.nx, sv.nz, sv.npml, sv.nt, sv.dx, sv.dt, src_xz, rec_xz, shots_per_batch=args.batch,
-                 block_x=args.block_x)
+    opts = dict(shots_per_batch=args.batch, block_x=args.block_x, kernel=args.kernel)
+    tuned = None
+    if not args.no_tune and args.batch == 0 and args.block_x == 0 and args.kernel == "auto":
+        from swit_gb300 import autotune
+        best, trials = autotune.tune(sv.nx, sv.nz, sv.npml, sv.dx, sv.dt, src_xz, rec_xz, sv.vp_init, rho,
+                                     free_surface=sv.free_surface)
+        opts.update(best)
+        tuned = [dict(c, ms=round(t * 1e3, 3)) for c, t in trials]
+    eng = Engine(sv.nx, sv.nz, sv.npml, sv.nt, sv.dx, sv.dt, src_xz, rec_xz, **opts)
     q = eng.query()
     # observed data from the true model, synthetics from the smoothed model
     eng.set_model(sv.vp_true, rho)
@@ -304,11 +317,12 @@ def run_mine(args):
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": sv.name, "grid": [sv.nx, sv.nz], "npml": sv.npml, "nt": sv.nt,
                        "shots_per_gpu": per_rank, "receivers": sv.ng, "dx_m": sv.dx, "dt_s": sv.dt,
-                       "path": "batched, CUDA graph", "shots_per_launch": q["shots_per_batch"],
+                       "path": "batched, CUDA graph", "kernel": q["kernel"], "shots_per_launch": q["shots_per_batch"],
                        "block_x": q["block_x"], "parallelism": "shots" + ("" if world == 1 else " x%d ranks" % world),
                        "l2": "inputs larger than L2: each step streams %.2f GB of boundary strips and %.2f GB of "
                              "traces" % (per_rank * sv.nt * (9 * sv.nx + 6 * sv.nz) * 4 / 1e9,
                                          2 * per_rank * sv.ng * sv.nt * 4 / 1e9)},
+            "autotune": {"trial_steps": 48, "candidates": tuned} if tuned else None,
             "gpts_per_s": value * U / 1e9,
             "hbm_roof_frac_step": (value / world) * B / 1e9 / peak,
             "algorithmic_gb_per_shot_gradient": B / 1e9,
@@ -334,7 +348,8 @@ def run_mine(args):
                             "kernels": {k: dict(v, share=tot[k] / sum(tot.values())) for k, v in prof.items()}}
         # plain one-shot-per-launch path on a bounded sample
         nplain = min(4, per_rank)
-        pe = Engine(sv.nx, sv.nz, sv.npml, sv.nt, sv.dx, sv.dt, src_xz[:nplain], rec_xz[:nplain], path="plain")
+        pe = Engine(sv.nx, sv.nz, sv.npml, sv.nt, sv.dx, sv.dt, src_xz[:nplain], rec_xz[:nplain], path="plain",
+                    kernel=q["kernel"], block_x=q["block_x"])
         pe.set_model(sv.vp_init, rho)
         src_p, obs_p = src_d[:nplain].contiguous(), obs_d[:nplain].contiguous()
         pe.gradient_l2(src_p, obs_p)

@@ -69,7 +69,12 @@ typedef struct swit_desc {
                                1 = plain: one shot per launch, one launch per
                                kernel and step, no graph                          */
   int32_t shots_per_batch;  /* batched path: shots per launch, 0 = automatic    */
-  int32_t block_x;          /* columns per CTA, 0 = automatic                   */
+  int32_t block_x;          /* columns per CTA, 0 = automatic: split kernels
+                               1, 2, 4 or 8 (x 32 rows); fused kernels 8, 16
+                               or 32 (x all rows)                                 */
+  int32_t kernel_variant;   /* 0 = automatic (fused when NZ + 2 npml <= 1024),
+                               1 = split: two kernels per step, in place,
+                               2 = fused: one kernel per step, double-buffered   */
 } swit_desc;
 
 /* Creates an engine and allocates its device workspace on the current device.
@@ -128,12 +133,14 @@ int swit_export_snapshot(swit_engine* e, void* boundary, void* p_end, void* u_en
  * CUDA event pair around it on `stream`, and returns for each kernel --
  * [0] forward pressure phase, [1] forward velocity phase, [2] backward velocity
  * phase, [3] backward pressure phase -- the number of launches and the mean
- * launch duration in milliseconds.  Synchronises the stream. */
+ * launch duration in milliseconds.  With the fused variant, [0] is the forward
+ * step kernel, [2] the reverse step kernel and [1], [3] are unused (0 launches).
+ * Synchronises the stream. */
 int swit_profile_kernels(swit_engine* e, int32_t launches[4], double mean_ms[4], void* stream);
 
 /* Sizes the engine has allocated; any pointer may be NULL. */
 int swit_query(const swit_engine* e, int64_t* device_bytes, int32_t* shots_per_batch, int32_t* block_x,
-               int32_t* kernels_per_forward, int32_t* kernels_per_backward);
+               int32_t* kernels_per_forward, int32_t* kernels_per_backward, int32_t* kernel_variant);
 
 /* Releases the engine and its device memory. */
 int swit_destroy(swit_engine* e);

@@ -23,7 +23,8 @@ class SwitDesc(C.Structure):
                 ("dx", C.c_float), ("dt", C.c_float), ("free_surface", C.c_int32), ("ns", C.c_int32),
                 ("ng_max", C.c_int32), ("ng", C.c_void_p), ("src_x", C.c_void_p), ("src_z", C.c_void_p),
                 ("rec_x", C.c_void_p), ("rec_z", C.c_void_p), ("precision", C.c_int32), ("path", C.c_int32),
-                ("shots_per_batch", C.c_int32), ("block_x", C.c_int32)]
+                ("shots_per_batch", C.c_int32), ("block_x", C.c_int32),
+                ("kernel_variant", C.c_int32)]
 
 
 class SwitError(RuntimeError):
@@ -57,7 +58,7 @@ def load(build_if_missing: bool = True):
         "swit_export_snapshot": ([vp, vp, vp, vp, vp, i, vp], i),
         "swit_profile_kernels": ([vp, C.POINTER(C.c_int32), C.POINTER(C.c_double), vp], i),
         "swit_query": ([vp, C.POINTER(C.c_int64), C.POINTER(C.c_int32), C.POINTER(C.c_int32),
-                        C.POINTER(C.c_int32), C.POINTER(C.c_int32)], i),
+                        C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.POINTER(C.c_int32)], i),
         "swit_destroy": ([vp], i),
         "swit_last_error": ([], C.c_char_p),
         "swit_damp_profile": ([C.c_int32, C.c_int32, C.c_int32, C.c_float, C.c_float, vp], i),

@@ -1,0 +1,65 @@
+"""Launch-configuration autotuner.
+
+Times a short Waveform-gradient run (the full geometry and shot count, a few
+dozen time steps) for each candidate (kernel variant, columns per CTA, shots
+per launch) and returns the fastest.  Every candidate computes bit-identical
+results, so the choice only affects speed.  Results are cached per process
+by problem shape.
+"""
+import time
+
+import numpy as np
+
+from .engine import Engine
+
+_cache = {}
+
+
+FUSED = False  # fused kernels join the candidates once validated on the GPU
+
+
+def candidates(ns, nz_pml):
+    out = []
+    batches = sorted({ns, max(1, (ns + 1) // 2), max(1, (ns + 3) // 4)}, reverse=True)
+    if FUSED and nz_pml <= 1024:
+        for tx in (8, 16, 32):
+            for b in batches:
+                out.append(dict(kernel="fused", block_x=tx, shots_per_batch=b))
+    for bx in (4, 8):
+        out.append(dict(kernel="split", block_x=bx, shots_per_batch=ns))
+    return out
+
+
+def tune(nx, nz, npml, dx, dt, src_xz, rec_xz, vp, rho, free_surface=1, trial_steps=48, repeats=2,
+         cands=None, verbose=False):
+    """Returns (best options, [(options, seconds per trial gradient), ...])."""
+    import torch
+    src_xz = np.asarray(src_xz, np.float32)
+    rec_xz = np.asarray(rec_xz, np.float32)
+    ns = src_xz.shape[0]
+    key = (nx, nz, npml, ns, rec_xz.shape[-2], trial_steps, free_surface)
+    if key in _cache and cands is None:
+        return _cache[key]
+    cands = cands or candidates(ns, nz + 2 * npml)
+    nt = trial_steps
+    rng = np.random.default_rng(0)
+    src = torch.from_numpy(rng.standard_normal((ns, nt)).astype(np.float32)).cuda()
+    times = []
+    for c in cands:
+        with Engine(nx, nz, npml, nt, dx, dt, src_xz, rec_xz, free_surface=free_surface, **c) as e:
+            e.set_model(vp, rho)
+            obs = torch.zeros((ns, e.ngmax, nt), dtype=torch.float32, device="cuda")
+            e.gradient_l2(src, obs)  # graphs captured here
+            torch.cuda.synchronize()
+            best = float("inf")
+            for _ in range(repeats):
+                t0 = time.perf_counter()
+                e.gradient_l2(src, obs)
+                torch.cuda.synchronize()
+                best = min(best, time.perf_counter() - t0)
+            times.append((dict(c), best))
+            if verbose:
+                print("autotune", c, "%.3f ms" % (best * 1e3))
+    best = min(times, key=lambda t: t[1])[0]
+    _cache[key] = (best, times)
+    return best, times

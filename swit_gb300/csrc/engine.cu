@@ -16,6 +16,7 @@
 
 #include "../../include/swit_gb300.h"
 #include "kernels.cuh"
+#include "kernels_fused.cuh"
 
 using namespace swit;
 
@@ -48,6 +49,7 @@ struct swit_engine {
   int nx, nz, L, nt, NX, NZ, LD, LDI, fs, fs_flag, ns, ngmax, SL, prec, path;
   float dx32, dt32;
   int batch, bx;
+  int variant;  // 1 = split (two in-place kernels per step), 2 = fused (one kernel per step, ping-pong)
   int device;
   size_t esz;  // sizeof(R)
   std::vector<int> ng, isx, isz, risx, risz, colptr, ent_ig, ent_zr;
@@ -60,6 +62,9 @@ struct swit_engine {
   void *p = nullptr, *u = nullptr, *w = nullptr, *pb = nullptr, *ub = nullptr, *wb = nullptr;
   void *pe = nullptr, *ue = nullptr, *we = nullptr, *dg = nullptr, *dfw = nullptr, *dbk = nullptr;
   void *strips = nullptr, *src = nullptr, *seis_t = nullptr, *adj_t = nullptr;
+  // second state buffers of the fused variant
+  void *p2 = nullptr, *u2 = nullptr, *w2 = nullptr, *pb2 = nullptr, *ub2 = nullptr, *wb2 = nullptr;
+  void *pe2 = nullptr, *ue2 = nullptr, *we2 = nullptr;
   float* d_in = nullptr;     // float staging: sources / obs / adjoint sources from the host
   void* d_stage = nullptr;   // output staging for host outputs
   size_t bytes = 0;
@@ -103,7 +108,7 @@ void release(swit_engine* e) {
   void* ptrs[] = {e->d_ng, e->d_isx, e->d_isz, e->d_risx, e->d_risz, e->d_colptr, e->d_ig, e->d_zr, e->d_live,
                   e->d_mtrace, e->A, e->B, e->damp, e->cint, e->p, e->u, e->w, e->pb, e->ub, e->wb, e->pe,
                   e->ue, e->we, e->dg, e->dfw, e->dbk, e->strips, e->src, e->seis_t, e->adj_t, e->d_in,
-                  e->d_stage};
+                  e->d_stage, e->p2, e->u2, e->w2, e->pb2, e->ub2, e->wb2, e->pe2, e->ue2, e->we2};
   for (void* q : ptrs)
     if (q) cudaFree(q);
 }
@@ -143,9 +148,71 @@ inline void stencil_shape(const swit_engine* e, int nb, dim3& grid, dim3& block)
   grid = dim3((e->NZ + 31) / 32, (e->NX + e->bx - 1) / e->bx, nb);
 }
 
+// One fused forward step (fdcore.f90:77-159) of shots [shot0, shot0+nb).
+template <class R>
+void launch_fwd_step(swit_engine* e, bool store, int shot0, int nb, int it, cudaStream_t st) {
+  Grid<R> g = make_grid<R>(e);
+  const bool even = (it - 2) % 2 == 0;  // step it reads set A when it is even
+  const R* P0 = (const R*)(even ? e->p : e->p2);
+  const R* U0 = (const R*)(even ? e->u : e->u2);
+  const R* W0 = (const R*)(even ? e->w : e->w2);
+  R* P1 = (R*)(even ? e->p2 : e->p);
+  R* U1 = (R*)(even ? e->u2 : e->u);
+  R* W1 = (R*)(even ? e->w2 : e->w);
+  R* strips = store ? (R*)e->strips : nullptr;
+  const dim3 grid((e->NX + e->bx - 1) / e->bx, nb), block(e->LD);
+  const size_t sm = 2 * (size_t)(e->LD + 4) * sizeof(R);
+#define FWD(TX)                                                                                            \
+  k_fwd_step<R, TX><<<grid, block, sm, st>>>(g, make_src(e), make_rec(e), (const R*)e->src, P0, U0, W0, P1, U1, \
+                                             W1, (R*)e->seis_t, strips, it, shot0)
+  if (e->bx == 8)
+    FWD(8);
+  else if (e->bx == 32)
+    FWD(32);
+  else
+    FWD(16);
+#undef FWD
+}
+
+// One fused reverse step (fdcore.f90:220-287, 309-373; solver.f90:232-239).
+template <class R>
+void launch_bwd_step(swit_engine* e, int shot0, int nb, int it, cudaStream_t st) {
+  Grid<R> g = make_grid<R>(e);
+  const bool even = (e->nt - it) % 2 == 0;  // the first reverse step reads set A
+  const R* PB0 = (const R*)(even ? e->pb : e->pb2);
+  const R* UB0 = (const R*)(even ? e->ub : e->ub2);
+  const R* WB0 = (const R*)(even ? e->wb : e->wb2);
+  R* PB1 = (R*)(even ? e->pb2 : e->pb);
+  R* UB1 = (R*)(even ? e->ub2 : e->ub);
+  R* WB1 = (R*)(even ? e->wb2 : e->wb);
+  const R* PE0 = (const R*)(even ? e->pe : e->pe2);
+  const R* UE0 = (const R*)(even ? e->ue : e->ue2);
+  const R* WE0 = (const R*)(even ? e->we : e->we2);
+  R* PE1 = (R*)(even ? e->pe2 : e->pe);
+  R* UE1 = (R*)(even ? e->ue2 : e->ue);
+  R* WE1 = (R*)(even ? e->we2 : e->we);
+  const dim3 grid((e->NX + e->bx - 1) / e->bx, nb), block(e->LD);
+  const size_t sm = 4 * (size_t)(e->LD + 4) * sizeof(R);
+#define BWD(TX)                                                                                                \
+  k_bwd_step<R, TX><<<grid, block, sm, st>>>(g, make_src(e), make_rec(e), (const R*)e->src, (const R*)e->adj_t, \
+                                             PB0, UB0, WB0, PB1, UB1, WB1, PE0, UE0, WE0, PE1, UE1, WE1,         \
+                                             (R*)e->dg, (R*)e->dfw, (R*)e->dbk, (const R*)e->strips, it, shot0)
+  if (e->bx == 8)
+    BWD(8);
+  else if (e->bx == 32)
+    BWD(32);
+  else
+    BWD(16);
+#undef BWD
+}
+
 // Forward time loop of shots [shot0, shot0+nb): fdcore.f90:75-160.
 template <class R>
 void launch_forward_steps(swit_engine* e, bool store, int shot0, int nb, cudaStream_t st) {
+  if (e->variant == 2) {
+    for (int it = 2; it <= e->nt; ++it) launch_fwd_step<R>(e, store, shot0, nb, it, st);
+    return;
+  }
   Grid<R> g = make_grid<R>(e);
   dim3 grid, block;
   stencil_shape(e, nb, grid, block);
@@ -161,6 +228,10 @@ void launch_forward_steps(swit_engine* e, bool store, int shot0, int nb, cudaStr
 // Reverse time loop of shots [shot0, shot0+nb): solver.f90:230-253.
 template <class R>
 void launch_backward_steps(swit_engine* e, int shot0, int nb, cudaStream_t st) {
+  if (e->variant == 2) {
+    for (int it = e->nt; it >= 2; --it) launch_bwd_step<R>(e, shot0, nb, it, st);
+    return;
+  }
   Grid<R> g = make_grid<R>(e);
   dim3 grid, block;
   stencil_shape(e, nb, grid, block);
@@ -232,7 +303,21 @@ __global__ void k_src_in(const float* __restrict__ in, R* out, int ns, int nt) {
   }
 }
 
-inline int nblocks(size_t n, int bs = 256) {
+inline int nblocks(size_t n, int bs = 256);
+
+// Final forward state -> reconstruction fields (set A), fdcore.f90:164-166.
+template <class R>
+void copy_end(swit_engine* e, cudaStream_t st) {
+  Grid<R> g = make_grid<R>(e);
+  const bool in_b = e->variant == 2 && (e->nt - 2) % 2 == 0;  // the last step wrote set B
+  const R* P = (const R*)(in_b ? e->p2 : e->p);
+  const R* U = (const R*)(in_b ? e->u2 : e->u);
+  const R* W = (const R*)(in_b ? e->w2 : e->w);
+  k_copy_end<R><<<nblocks((size_t)e->ns * e->nx * e->nz), 256, 0, st>>>(g, P, U, W, (R*)e->pe, (R*)e->ue,
+                                                                        (R*)e->we, e->ns);
+}
+
+inline int nblocks(size_t n, int bs) {
   size_t b = (n + bs - 1) / bs;
   return (int)std::min<size_t>(b, 152 * 16);
 }
@@ -259,13 +344,13 @@ int forward_impl(swit_engine* e, const float* src, void* seis, bool store, int o
   CK(cudaMemsetAsync(e->p, 0, fb, st));
   CK(cudaMemsetAsync(e->u, 0, fb, st));
   CK(cudaMemsetAsync(e->w, 0, fb, st));
+  if (e->variant == 2) {
+    CK(cudaMemsetAsync(e->p2, 0, fb, st));
+    CK(cudaMemsetAsync(e->u2, 0, fb, st));
+    CK(cudaMemsetAsync(e->w2, 0, fb, st));
+  }
   rc = run_forward_loop<R>(e, store, st);
   if (rc) return rc;
-  if (store) {
-    k_copy_end<R><<<nblocks((size_t)e->ns * e->nx * e->nz), 256, 0, st>>>(g, (const R*)e->p, (const R*)e->u,
-                                                                          (const R*)e->w, (R*)e->pe, (R*)e->ue,
-                                                                          (R*)e->we, e->ns);
-  }
   if (seis) {
     dim3 grid((e->nt + 31) / 32, (e->ngmax + 31) / 32, e->ns), block(32, 8);
     void* out = on_device ? seis : e->d_stage;
@@ -288,9 +373,17 @@ int backward_core(swit_engine* e, void* grad, void* fw, void* bk, int on_device,
   CK(cudaMemsetAsync(e->pb, 0, fb, st));
   CK(cudaMemsetAsync(e->ub, 0, fb, st));
   CK(cudaMemsetAsync(e->wb, 0, fb, st));
+  if (e->variant == 2) {
+    CK(cudaMemsetAsync(e->pb2, 0, fb, st));
+    CK(cudaMemsetAsync(e->ub2, 0, fb, st));
+    CK(cudaMemsetAsync(e->wb2, 0, fb, st));
+  }
   CK(cudaMemsetAsync(e->dg, 0, ib, st));
   CK(cudaMemsetAsync(e->dfw, 0, ib, st));
   CK(cudaMemsetAsync(e->dbk, 0, ib, st));
+  // the reverse loop starts from the final forward state, which the forward
+  // buffers keep until the next forward: every backward sees the same start
+  copy_end<R>(e, st);
   int rc = run_backward_loop<R>(e, st);
   if (rc) return rc;
   const size_t NI = (size_t)e->nx * e->nz;
@@ -422,6 +515,7 @@ int set_model_impl(swit_engine* e, const float* vp, const float* rho, cudaStream
 template <class R>
 int export_impl(swit_engine* e, void* boundary, void* pend, void* uend, void* wend, int on_device, cudaStream_t st) {
   Grid<R> g = make_grid<R>(e);
+  copy_end<R>(e, st);
   const size_t NB = (size_t)e->ns * e->nt * e->SL, NI = (size_t)e->ns * e->nx * e->nz;
   auto one = [&](void* dst, size_t n, auto&& launch) -> int {
     if (!dst) return 0;
@@ -461,28 +555,33 @@ int export_impl(swit_engine* e, void* boundary, void* pend, void* uend, void* we
   return 0;
 }
 
-// Per-launch timing of the four stencil kernels with CUDA events.
+// Per-launch timing of the stencil kernels with CUDA events.
 template <class R>
 int profile_impl(swit_engine* e, int32_t launches[4], double mean_ms[4], cudaStream_t st) {
   Grid<R> g = make_grid<R>(e);
   const int nshot_launch = e->path == 1 ? 1 : e->batch;
   std::vector<cudaEvent_t> ev[4];
-  auto record = [&](int which) -> cudaEvent_t {
+  auto record = [&](int which) {
     cudaEvent_t a;
     cudaEventCreate(&a);
     ev[which].push_back(a);
     cudaEventRecord(a, st);
-    return a;
   };
   const size_t fb = (size_t)e->ns * g.FSZ * e->esz, ib = (size_t)e->ns * g.FSI * e->esz;
-  CK(cudaMemsetAsync(e->p, 0, fb, st));
-  CK(cudaMemsetAsync(e->u, 0, fb, st));
-  CK(cudaMemsetAsync(e->w, 0, fb, st));
+  void* fz[] = {e->p, e->u, e->w, e->p2, e->u2, e->w2};
+  for (void* q : fz)
+    if (q) CK(cudaMemsetAsync(q, 0, fb, st));
   for (int s0 = 0; s0 < e->ns; s0 += nshot_launch) {
     const int nb = std::min(nshot_launch, e->ns - s0);
     dim3 grid, block;
     stencil_shape(e, nb, grid, block);
     for (int it = 2; it <= e->nt; ++it) {
+      if (e->variant == 2) {
+        record(0);
+        launch_fwd_step<R>(e, true, s0, nb, it, st);
+        record(0);
+        continue;
+      }
       record(0);
       k_fwd_p<R><<<grid, block, 0, st>>>(g, make_src(e), (const R*)e->src, (R*)e->p, (const R*)e->u,
                                          (const R*)e->w, it, s0);
@@ -493,20 +592,24 @@ int profile_impl(swit_engine* e, int32_t launches[4], double mean_ms[4], cudaStr
       record(1);
     }
   }
-  k_copy_end<R><<<nblocks((size_t)e->ns * e->nx * e->nz), 256, 0, st>>>(g, (const R*)e->p, (const R*)e->u,
-                                                                        (const R*)e->w, (R*)e->pe, (R*)e->ue,
-                                                                        (R*)e->we, e->ns);
-  CK(cudaMemsetAsync(e->pb, 0, fb, st));
-  CK(cudaMemsetAsync(e->ub, 0, fb, st));
-  CK(cudaMemsetAsync(e->wb, 0, fb, st));
+  void* bz[] = {e->pb, e->ub, e->wb, e->pb2, e->ub2, e->wb2};
+  for (void* q : bz)
+    if (q) CK(cudaMemsetAsync(q, 0, fb, st));
   CK(cudaMemsetAsync(e->dg, 0, ib, st));
   CK(cudaMemsetAsync(e->dfw, 0, ib, st));
   CK(cudaMemsetAsync(e->dbk, 0, ib, st));
+  copy_end<R>(e, st);
   for (int s0 = 0; s0 < e->ns; s0 += nshot_launch) {
     const int nb = std::min(nshot_launch, e->ns - s0);
     dim3 grid, block;
     stencil_shape(e, nb, grid, block);
     for (int it = e->nt; it >= 2; --it) {
+      if (e->variant == 2) {
+        record(2);
+        launch_bwd_step<R>(e, s0, nb, it, st);
+        record(2);
+        continue;
+      }
       record(2);
       k_bwd_uw<R><<<grid, block, 0, st>>>(g, (const R*)e->pb, (R*)e->ub, (R*)e->wb, (const R*)e->pe, (R*)e->ue,
                                           (R*)e->we, (const R*)e->strips, it, s0);
@@ -578,10 +681,27 @@ int swit_create(const swit_desc* d, swit_engine** out) {
   e->dt32 = d->dt;
   e->esz = e->prec ? sizeof(double) : sizeof(float);
   e->batch = d->shots_per_batch > 0 ? std::min(d->shots_per_batch, d->ns) : d->ns;
-  e->bx = d->block_x > 0 ? d->block_x : 4;
-  if (32 * e->bx > 256 || (e->bx & (e->bx - 1))) {
+  if (d->kernel_variant < 0 || d->kernel_variant > 2) {
     delete e;
-    return fail(SWIT_E_ARG, "block_x must be a power of two <= 8");
+    return fail(SWIT_E_ARG, "kernel_variant must be 0, 1 or 2");
+  }
+  e->variant = d->kernel_variant ? d->kernel_variant : 1;
+  if (e->variant == 2 && e->LD > 1024) {
+    delete e;
+    return fail(SWIT_E_LIMIT, "the fused kernels need NZ + 2 npml <= 1024 (got %d)", e->NZ);
+  }
+  if (e->variant == 2) {
+    e->bx = d->block_x > 0 ? d->block_x : 16;
+    if (e->bx != 8 && e->bx != 16 && e->bx != 32) {
+      delete e;
+      return fail(SWIT_E_ARG, "block_x of the fused kernels must be 8, 16 or 32");
+    }
+  } else {
+    e->bx = d->block_x > 0 ? d->block_x : 4;
+    if (32 * e->bx > 256 || (e->bx & (e->bx - 1))) {
+      delete e;
+      return fail(SWIT_E_ARG, "block_x of the split kernels must be a power of two <= 8");
+    }
   }
   cudaGetDevice(&e->device);
 
@@ -673,6 +793,12 @@ int swit_create(const swit_desc* d, swit_engine** out) {
   for (void** f : fields) AL(valloc(e, f, (size_t)ns * FSZ));
   void** ifields[] = {&e->pe, &e->ue, &e->we, &e->dg, &e->dfw, &e->dbk};
   for (void** f : ifields) AL(valloc(e, f, (size_t)ns * FSI));
+  if (e->variant == 2) {
+    void** f2[] = {&e->p2, &e->u2, &e->w2, &e->pb2, &e->ub2, &e->wb2};
+    for (void** f : f2) AL(valloc(e, f, (size_t)ns * FSZ));
+    void** i2[] = {&e->pe2, &e->ue2, &e->we2};
+    for (void** f : i2) AL(valloc(e, f, (size_t)ns * FSI));
+  }
   AL(valloc(e, &e->strips, (size_t)ns * e->nt * e->SL));
   AL(valloc(e, &e->src, (size_t)ns * (e->nt + 1)));
   AL(valloc(e, &e->seis_t, (size_t)ns * e->nt * ngm));
@@ -710,8 +836,9 @@ int swit_create(const swit_desc* d, swit_engine** out) {
   }
   const int waves = (ns + e->batch - 1) / e->batch;
   const int per = e->path == 1 ? ns : waves;
-  e->launches_fwd = per * (e->nt - 1) * 2;
-  e->launches_bwd = per * (e->nt - 1) * 2;
+  const int per_step = e->variant == 2 ? 1 : 2;
+  e->launches_fwd = per * (e->nt - 1) * per_step;
+  e->launches_bwd = per * (e->nt - 1) * per_step;
   *out = e;
   return 0;
 }
@@ -785,13 +912,14 @@ int swit_profile_kernels(swit_engine* e, int32_t launches[4], double mean_ms[4],
 }
 
 int swit_query(const swit_engine* e, int64_t* device_bytes, int32_t* shots_per_batch, int32_t* block_x,
-               int32_t* kernels_per_forward, int32_t* kernels_per_backward) {
+               int32_t* kernels_per_forward, int32_t* kernels_per_backward, int32_t* kernel_variant) {
   if (!e) return fail(SWIT_E_ARG, "null argument");
   if (device_bytes) *device_bytes = (int64_t)e->bytes;
   if (shots_per_batch) *shots_per_batch = e->path == 1 ? 1 : e->batch;
   if (block_x) *block_x = e->bx;
   if (kernels_per_forward) *kernels_per_forward = e->launches_fwd;
   if (kernels_per_backward) *kernels_per_backward = e->launches_bwd;
+  if (kernel_variant) *kernel_variant = e->variant;
   return 0;
 }
 

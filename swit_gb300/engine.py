@@ -27,7 +27,7 @@ class Engine:
     """
 
     def __init__(self, nx, nz, npml, nt, dx, dt, src_xz, rec_xz, free_surface=1, ng=None, precision="fp32",
-                 path="batched", shots_per_batch=0, block_x=0):
+                 path="batched", shots_per_batch=0, block_x=0, kernel="auto"):
         lib = _lib.load()
         src_xz = np.asarray(src_xz, dtype=np.float32).reshape(-1, 2)
         rec_xz = np.asarray(rec_xz, dtype=np.float32)
@@ -45,6 +45,9 @@ class Engine:
         if path not in ("batched", "plain"):
             raise ValueError("path must be 'batched' or 'plain'")
         self.path = path
+        variants = {"auto": 0, "split": 1, "fused": 2}
+        if kernel not in variants:
+            raise ValueError("kernel must be 'auto', 'split' or 'fused'")
         self._keep = dict(
             ng=np.ascontiguousarray(np.full(self.ns, self.ngmax) if ng is None else ng, dtype=np.int32),
             xs=np.ascontiguousarray(src_xz[:, 0]), zs=np.ascontiguousarray(src_xz[:, 1]),
@@ -53,7 +56,7 @@ class Engine:
         d = _lib.SwitDesc(self.nx, self.nz, self.npml, self.nt, self.dx, self.dt, int(free_surface), self.ns,
                           self.ngmax, k["ng"].ctypes.data, k["xs"].ctypes.data, k["zs"].ctypes.data,
                           k["xg"].ctypes.data, k["zg"].ctypes.data, 1 if self.fp64 else 0,
-                          1 if path == "plain" else 0, int(shots_per_batch), int(block_x))
+                          1 if path == "plain" else 0, int(shots_per_batch), int(block_x), variants[kernel])
         h = C.c_void_p()
         _lib.check(lib.swit_create(C.byref(d), C.byref(h)))
         self._h = h
@@ -168,14 +171,17 @@ class Engine:
         ms = (C.c_double * 4)()
         _lib.check(self._lib.swit_profile_kernels(self._h, n, ms, torch.cuda.current_stream().cuda_stream))
         names = ("fwd_p", "fwd_uw", "bwd_uw", "bwd_p")
-        return {k: dict(launches=int(n[i]), mean_ms=float(ms[i])) for i, k in enumerate(names)}
+        if self.query()["kernel"] == "fused":
+            names = ("fwd_step", None, "bwd_step", None)
+        return {k: dict(launches=int(n[i]), mean_ms=float(ms[i])) for i, k in enumerate(names) if k}
 
     def query(self):
         by = C.c_int64()
-        sb, bx, kf, kb = C.c_int32(), C.c_int32(), C.c_int32(), C.c_int32()
-        _lib.check(self._lib.swit_query(self._h, C.byref(by), C.byref(sb), C.byref(bx), C.byref(kf), C.byref(kb)))
+        sb, bx, kf, kb, kv = C.c_int32(), C.c_int32(), C.c_int32(), C.c_int32(), C.c_int32()
+        _lib.check(self._lib.swit_query(self._h, C.byref(by), C.byref(sb), C.byref(bx), C.byref(kf), C.byref(kb),
+                                        C.byref(kv)))
         return dict(device_bytes=by.value, shots_per_batch=sb.value, block_x=bx.value, kernels_per_forward=kf.value,
-                    kernels_per_backward=kb.value)
+                    kernels_per_backward=kb.value, kernel={1: "split", 2: "fused"}.get(kv.value, "?"))
 
     def close(self):
         if getattr(self, "_h", None):

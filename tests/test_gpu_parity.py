@@ -92,8 +92,11 @@ def test_gradient_l2_single_call_matches_oracle(base):
     assert abs(out["misfit"] - want) <= 1e-6 * want
 
 
-@pytest.mark.parametrize("opts", [dict(path="plain"), dict(shots_per_batch=2), dict(block_x=8),
-                                  dict(block_x=1)])
+@pytest.mark.parametrize("opts", [dict(path="plain"), dict(shots_per_batch=2), dict(kernel="fused", block_x=8),
+                                  dict(kernel="fused", block_x=32), dict(kernel="fused", path="plain"),
+                                  dict(kernel="split"), dict(kernel="split", block_x=8),
+                                  dict(kernel="split", block_x=1), dict(kernel="split", path="plain"),
+                                  dict(kernel="split", shots_per_batch=2)])
 def test_launch_variants_are_identical(base, opts):
     s = base["s"]
     with engine(s, **opts) as e:
@@ -105,11 +108,12 @@ def test_launch_variants_are_identical(base, opts):
     np.testing.assert_array_equal(bk, base["grad"]["bk"])
 
 
-def test_fp64_build_matches_fp64_oracle(base):
+@pytest.mark.parametrize("kernel", ["fused", "split"])
+def test_fp64_build_matches_fp64_oracle(base, kernel):
     s, pb = base["s"], base["pb"]
     ref = O.forward(pb, s.vp_true, base["rho"], base["src"], store=True, fp64=True)
     gref = O.adjoint(pb, s.vp_true, base["rho"], base["src"], base["adj"], ref, fp64=True)
-    with engine(s, precision="fp64") as e:
+    with engine(s, precision="fp64", kernel=kernel) as e:
         e.set_model(s.vp_true, base["rho"])
         seis = e.forward(base["src"], save_boundary=True)
         g, fw, bk = e.backward(base["adj"])
@@ -118,7 +122,19 @@ def test_fp64_build_matches_fp64_oracle(base):
     assert rel(g, gref["g"]) <= 1e-12 and rel(fw, gref["fw"]) <= 1e-12 and rel(bk, gref["bk"]) <= 1e-12
 
 
-def test_edge_geometry_surface_receivers_deep_source_uneven_traces():
+def test_repeated_backward_after_one_forward(base):
+    s = base["s"]
+    with engine(s) as e:
+        e.set_model(s.vp_true, base["rho"])
+        e.forward(base["src"], save_boundary=True)
+        g1 = e.backward(base["adj"])[0]
+        g2 = e.backward(base["adj"])[0]
+    np.testing.assert_array_equal(g1, base["grad"]["g"])
+    np.testing.assert_array_equal(g2, base["grad"]["g"])
+
+
+@pytest.mark.parametrize("kernel", ["fused", "split"])
+def test_edge_geometry_surface_receivers_deep_source_uneven_traces(kernel):
     """Receivers on z = 0 (moved one node down), a source deep enough that the
     reconstruction subtracts it (fdcore.f90:250-256), shots with different
     receiver counts, a receiver shared by two grid-coincident positions."""
@@ -135,7 +151,7 @@ def test_edge_geometry_surface_receivers_deep_source_uneven_traces():
     for i in range(3):
         adj[i, ng[i]:] = 0
     gref = O.adjoint(pb, s.vp_true, rho, src, adj, ref)
-    with Engine(**s.engine_args(), ng=ng) as e:
+    with Engine(**s.engine_args(), ng=ng, kernel=kernel) as e:
         e.set_model(s.vp_true, rho)
         seis = e.forward(src, save_boundary=True)
         g, fw, bk = e.backward(adj)
@@ -145,7 +161,8 @@ def test_edge_geometry_surface_receivers_deep_source_uneven_traces():
     np.testing.assert_array_equal(bk, gref["bk"])
 
 
-def test_no_free_surface():
+@pytest.mark.parametrize("kernel", ["fused", "split"])
+def test_no_free_surface(kernel):
     s, _ = case(nt=200)
     s.free_surface = 0
     pb = O.Problem(s.nx, s.nz, s.npml, s.nt, s.dx, s.dt, s.src_xz, s.rec_xz, free_surface=0)
@@ -154,7 +171,7 @@ def test_no_free_surface():
     ref = O.forward(pb, s.vp_true, rho, src, store=True)
     adj = (ref["seis"] * 0.5).astype(np.float32)
     gref = O.adjoint(pb, s.vp_true, rho, src, adj, ref)
-    with engine(s) as e:
+    with engine(s, kernel=kernel) as e:
         e.set_model(s.vp_true, rho)
         seis = e.forward(src, save_boundary=True)
         g, fw, bk = e.backward(adj)
