@@ -33,6 +33,7 @@ def test_dropin_forward_and_adjoint_files_match_oracle(tmp_path):
     simu = _simu(tmp_path, s, s.vp_true)
     solver.forward(simu, "obs", savesnap=0)
     simu.model.vp = s.vp_init.astype(np.float64)
+    simu.model.rho = s.rho(s.vp_init).astype(np.float64)
     solver.forward(simu, "syn", savesnap=1)
     home = simu.system.homepath
     # oracle with the values fd2dmpi parses from the files
