@@ -138,6 +138,32 @@ int swit_export_snapshot(swit_engine* e, void* boundary, void* p_end, void* u_en
  * Synchronises the stream. */
 int swit_profile_kernels(swit_engine* e, int32_t launches[4], double mean_ms[4], void* stream);
 
+/* Capacity of swit_forward_shot_static's fixed scratch (about 2.7 MB per GPU). */
+#define SWIT_STATIC_MAX_POINTS 131072 /* (nx + 2 npml) x round_up(nz + 2 npml, 32) */
+#define SWIT_STATIC_MAX_COLUMNS 4096  /* nx + 2 npml                             */
+#define SWIT_STATIC_MAX_RECEIVERS 4096
+#define SWIT_STATIC_MAX_NPML 256
+
+/* No counterpart in the reference.  Forward modeling of ONE shot that
+ * allocates no device memory, for callers that cannot call cudaMalloc: a host
+ * framework or plugin host that owns all device memory through its own pool, or
+ * a loop that cannot afford the device-wide synchronisation of cudaMalloc and
+ * cudaFree.  Its wavefields, coefficients and receiver table live in one
+ * file-scope static device array of fixed size (SWIT_STATIC_*; every GPU that
+ * loads this library holds it until the process exits); larger problems are
+ * rejected with SWIT_E_LIMIT before any GPU work.  vp, rho (nx, nz), src (nt)
+ * and seis (ng, nt) are DEVICE arrays; rec_x, rec_z (ng) are host arrays.
+ * Results equal swit_forward's for the same shot.  The first call on a device
+ * looks up the array's device address (cudaGetSymbolAddress) -- make it before
+ * any stream capture.  The wavefields are cleared on every call; all calls on a
+ * device share the array, so calls that overlap on the GPU race.  The call is
+ * ordered on `stream` and returns once the launches are queued; dt is not
+ * checked against the CFL limit (the model stays on the device). */
+int swit_forward_shot_static(int32_t nx, int32_t nz, int32_t npml, int32_t nt, float dx, float dt,
+                             int32_t free_surface, float src_x, float src_z, int32_t ng, const float* rec_x,
+                             const float* rec_z, const float* vp, const float* rho, const float* src, float* seis,
+                             void* stream);
+
 /* Sizes the engine has allocated; any pointer may be NULL. */
 int swit_query(const swit_engine* e, int64_t* device_bytes, int32_t* shots_per_batch, int32_t* block_x,
                int32_t* kernels_per_forward, int32_t* kernels_per_backward, int32_t* kernel_variant);

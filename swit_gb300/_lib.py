@@ -15,7 +15,8 @@ ERRORS = {-1: "SWIT_E_ARG", -2: "SWIT_E_GEOM", -3: "SWIT_E_CFL", -4: "SWIT_E_MOD
 
 # every symbol include/swit_gb300.h declares
 EXPORTS = ("swit_create", "swit_set_model", "swit_forward", "swit_backward", "swit_gradient_l2",
-           "swit_export_snapshot", "swit_profile_kernels", "swit_query", "swit_destroy", "swit_last_error", "swit_damp_profile")
+           "swit_export_snapshot", "swit_profile_kernels", "swit_query", "swit_destroy", "swit_last_error", "swit_damp_profile",
+           "swit_forward_shot_static")
 
 
 class SwitDesc(C.Structure):
@@ -62,6 +63,8 @@ def load(build_if_missing: bool = True):
         "swit_destroy": ([vp], i),
         "swit_last_error": ([], C.c_char_p),
         "swit_damp_profile": ([C.c_int32, C.c_int32, C.c_int32, C.c_float, C.c_float, vp], i),
+        "swit_forward_shot_static": ([C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_float, C.c_float, C.c_int32,
+                                      C.c_float, C.c_float, C.c_int32, vp, vp, vp, vp, vp, vp, vp], i),
     }
     for name, (args, res) in sig.items():
         f = getattr(lib, name)

@@ -1,6 +1,6 @@
 """Builds the engine library ``swit_gb300/libswit_gb300.so`` for sm_103a.
 
-One translation unit (csrc/engine.cu), one ``-gencode``; static cudart so the
+Two translation units (csrc/engine.cu, csrc/noalloc.cu), one ``-gencode``; static cudart so the
 library needs nothing but the driver at run time.  ``--fmad=false`` and the host
 ``-ffp-contract=off`` keep the reference's floating-point evaluation order
 (no fused multiply-add is formed on either side), which makes FP32 results
@@ -37,7 +37,8 @@ def build(force: bool = False, verbose: bool = False, extra=()) -> str:
     newest = max(os.path.getmtime(s) for s in sources())
     if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= newest and not extra:
         return LIB
-    cmd = [_nvcc()] + NVCC_FLAGS + list(extra) + ["-o", LIB + ".tmp", os.path.join(CSRC, "engine.cu")]
+    units = [os.path.join(CSRC, f) for f in ("engine.cu", "noalloc.cu")]
+    cmd = [_nvcc()] + NVCC_FLAGS + list(extra) + ["-o", LIB + ".tmp"] + units
     if verbose:
         print(" ".join(cmd))
     subprocess.run(cmd, check=True)

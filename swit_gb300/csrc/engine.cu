@@ -44,6 +44,11 @@ inline int round_up(int a, int m) { return (a + m - 1) / m * m; }
 
 }  // namespace
 
+namespace swit {
+// Lets other translation units of the library report through swit_last_error.
+void set_last_error(const char* msg) { g_err = msg; }
+}  // namespace swit
+
 struct swit_engine {
   // problem
   int nx, nz, L, nt, NX, NZ, LD, LDI, fs, fs_flag, ns, ngmax, SL, prec, path;
