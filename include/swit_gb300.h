@@ -71,10 +71,11 @@ typedef struct swit_desc {
   int32_t shots_per_batch;  /* batched path: shots per launch, 0 = automatic    */
   int32_t block_x;          /* columns per CTA, 0 = automatic: split kernels
                                1, 2, 4 or 8 (x 32 rows); fused kernels 8, 16
-                               or 32 (x all rows)                                 */
-  int32_t kernel_variant;   /* 0 = automatic (fused when NZ + 2 npml <= 1024),
-                               1 = split: two kernels per step, in place,
-                               2 = fused: one kernel per step, double-buffered   */
+                               or 32 (x all rows); ignored by vec                */
+  int32_t kernel_variant;   /* 0 = automatic (vec), 1 = split: two kernels per step,
+                               in place, one point per thread; 2 = fused: one
+                               kernel per step, double-buffered (NZ + 2 npml <=
+                               1024); 3 = vec: split, four rows per thread      */
 } swit_desc;
 
 /* Creates an engine and allocates its device workspace on the current device.

@@ -17,6 +17,7 @@
 #include "../../include/swit_gb300.h"
 #include "kernels.cuh"
 #include "kernels_fused.cuh"
+#include "kernels_vec.cuh"
 
 using namespace swit;
 
@@ -54,7 +55,8 @@ struct swit_engine {
   int nx, nz, L, nt, NX, NZ, LD, LDI, fs, fs_flag, ns, ngmax, SL, prec, path;
   float dx32, dt32;
   int batch, bx;
-  int variant;  // 1 = split (two in-place kernels per step), 2 = fused (one kernel per step, ping-pong)
+  int variant;  // 1 = split, 2 = fused (one kernel per step, ping-pong), 3 = vec (split, 4 rows per thread)
+  int IL;       // interior fields: row/column offset into their layout (npml for vec, else 0)
   int device;
   size_t esz;  // sizeof(R)
   std::vector<int> ng, isx, isz, risx, risz, colptr, ent_ig, ent_zr;
@@ -134,7 +136,9 @@ Grid<R> make_grid(const swit_engine* e) {
   g.ngmax = e->ngmax;
   g.SL = e->SL;
   g.FSZ = (size_t)e->NX * e->LD;
-  g.FSI = (size_t)e->nx * e->LDI;
+  g.FSI = e->variant == 3 ? g.FSZ : (size_t)e->nx * e->LDI;
+  g.IL = e->IL;
+  if (e->variant == 3) g.LDI = e->LD;
   g.dt = (R)e->dt32;
   g.c1 = R(9.0) / R(8.0);    // global.f90:34
   g.c2 = R(-1.0) / R(24.0);  // global.f90:35
@@ -211,9 +215,25 @@ void launch_bwd_step(swit_engine* e, int shot0, int nb, int it, cudaStream_t st)
 #undef BWD
 }
 
+inline dim3 vec_grid(const swit_engine* e, int nb) {
+  return dim3((unsigned)(((size_t)e->NX * (e->LD / 4) + 255) / 256), nb);
+}
+
 // Forward time loop of shots [shot0, shot0+nb): fdcore.f90:75-160.
 template <class R>
 void launch_forward_steps(swit_engine* e, bool store, int shot0, int nb, cudaStream_t st) {
+  if (e->variant == 3) {
+    Grid<R> g = make_grid<R>(e);
+    R* strips = store ? (R*)e->strips : nullptr;
+    const dim3 grid = vec_grid(e, nb);
+    for (int it = 2; it <= e->nt; ++it) {
+      k_fwd_p_v<R><<<grid, 256, 0, st>>>(g, make_src(e), (const R*)e->src, (R*)e->p, (const R*)e->u, (const R*)e->w,
+                                         it, shot0);
+      k_fwd_uw_v<R><<<grid, 256, 0, st>>>(g, make_rec(e), (const R*)e->p, (R*)e->u, (R*)e->w, (R*)e->seis_t, strips,
+                                          it, shot0);
+    }
+    return;
+  }
   if (e->variant == 2) {
     for (int it = 2; it <= e->nt; ++it) launch_fwd_step<R>(e, store, shot0, nb, it, st);
     return;
@@ -233,6 +253,19 @@ void launch_forward_steps(swit_engine* e, bool store, int shot0, int nb, cudaStr
 // Reverse time loop of shots [shot0, shot0+nb): solver.f90:230-253.
 template <class R>
 void launch_backward_steps(swit_engine* e, int shot0, int nb, cudaStream_t st) {
+  if (e->variant == 3) {
+    Grid<R> g = make_grid<R>(e);
+    const dim3 grid = vec_grid(e, nb);
+    for (int it = e->nt; it >= 2; --it) {
+      k_bwd_uw_v<R><<<grid, 256, 0, st>>>(g, (const R*)e->pb, (R*)e->ub, (R*)e->wb, (const R*)e->pe, (R*)e->ue,
+                                          (R*)e->we, (const R*)e->strips, it, shot0);
+      k_bwd_p_v<R><<<grid, 256, 0, st>>>(g, make_rec(e), make_src(e), (const R*)e->src, (const R*)e->adj_t,
+                                         (R*)e->pb, (const R*)e->ub, (const R*)e->wb, (R*)e->pe, (const R*)e->ue,
+                                         (const R*)e->we, (R*)e->dg, (R*)e->dfw, (R*)e->dbk, (const R*)e->strips, it,
+                                         shot0);
+    }
+    return;
+  }
   if (e->variant == 2) {
     for (int it = e->nt; it >= 2; --it) launch_bwd_step<R>(e, shot0, nb, it, st);
     return;
@@ -498,7 +531,9 @@ int set_model_impl(swit_engine* e, const float* vp, const float* rho, cudaStream
       damp[i] = kappa * xa * xa;
     }
   }
-  std::vector<R> A((size_t)NX * LD, R(0)), B((size_t)NX * LD, R(0)), ci((size_t)nx * e->LDI, R(1));
+  const int LDI = e->variant == 3 ? LD : e->LDI, IL = e->IL;
+  const size_t nci = e->variant == 3 ? (size_t)NX * LD : (size_t)nx * e->LDI;
+  std::vector<R> A((size_t)NX * LD, R(0)), B((size_t)NX * LD, R(0)), ci(nci, R(1));
   for (int ix = 1; ix <= NX; ++ix)
     for (int iz = 1; iz <= NZ; ++iz) {
       const R dn = at(den, iz, ix), cc = at(c, iz, ix);
@@ -506,7 +541,7 @@ int set_model_impl(swit_engine* e, const float* vp, const float* rho, cudaStream
       B[(size_t)(ix - 1) * LD + (iz - 1)] = dt / (dn * dx);          // fdcore.f90:99
     }
   for (int jx = 1; jx <= nx; ++jx)
-    for (int jz = 1; jz <= nz; ++jz) ci[(size_t)(jx - 1) * e->LDI + (jz - 1)] = at(c, L + jz, L + jx);
+    for (int jz = 1; jz <= nz; ++jz) ci[(size_t)(jx - 1 + IL) * LDI + (jz - 1 + IL)] = at(c, L + jz, L + jx);
   CK(cudaMemcpyAsync(e->A, A.data(), A.size() * sizeof(R), cudaMemcpyHostToDevice, st));
   CK(cudaMemcpyAsync(e->B, B.data(), B.size() * sizeof(R), cudaMemcpyHostToDevice, st));
   CK(cudaMemcpyAsync(e->damp, damp.data(), damp.size() * sizeof(R), cudaMemcpyHostToDevice, st));
@@ -587,6 +622,18 @@ int profile_impl(swit_engine* e, int32_t launches[4], double mean_ms[4], cudaStr
         record(0);
         continue;
       }
+      if (e->variant == 3) {
+        const dim3 vg = vec_grid(e, nb);
+        record(0);
+        k_fwd_p_v<R><<<vg, 256, 0, st>>>(g, make_src(e), (const R*)e->src, (R*)e->p, (const R*)e->u, (const R*)e->w,
+                                         it, s0);
+        record(0);
+        record(1);
+        k_fwd_uw_v<R><<<vg, 256, 0, st>>>(g, make_rec(e), (const R*)e->p, (R*)e->u, (R*)e->w, (R*)e->seis_t,
+                                          (R*)e->strips, it, s0);
+        record(1);
+        continue;
+      }
       record(0);
       k_fwd_p<R><<<grid, block, 0, st>>>(g, make_src(e), (const R*)e->src, (R*)e->p, (const R*)e->u,
                                          (const R*)e->w, it, s0);
@@ -613,6 +660,20 @@ int profile_impl(swit_engine* e, int32_t launches[4], double mean_ms[4], cudaStr
         record(2);
         launch_bwd_step<R>(e, s0, nb, it, st);
         record(2);
+        continue;
+      }
+      if (e->variant == 3) {
+        const dim3 vg = vec_grid(e, nb);
+        record(2);
+        k_bwd_uw_v<R><<<vg, 256, 0, st>>>(g, (const R*)e->pb, (R*)e->ub, (R*)e->wb, (const R*)e->pe, (R*)e->ue,
+                                          (R*)e->we, (const R*)e->strips, it, s0);
+        record(2);
+        record(3);
+        k_bwd_p_v<R><<<vg, 256, 0, st>>>(g, make_rec(e), make_src(e), (const R*)e->src, (const R*)e->adj_t,
+                                         (R*)e->pb, (const R*)e->ub, (const R*)e->wb, (R*)e->pe, (const R*)e->ue,
+                                         (const R*)e->we, (R*)e->dg, (R*)e->dfw, (R*)e->dbk, (const R*)e->strips,
+                                         it, s0);
+        record(3);
         continue;
       }
       record(2);
@@ -686,11 +747,11 @@ int swit_create(const swit_desc* d, swit_engine** out) {
   e->dt32 = d->dt;
   e->esz = e->prec ? sizeof(double) : sizeof(float);
   e->batch = d->shots_per_batch > 0 ? std::min(d->shots_per_batch, d->ns) : d->ns;
-  if (d->kernel_variant < 0 || d->kernel_variant > 2) {
+  if (d->kernel_variant < 0 || d->kernel_variant > 3) {
     delete e;
-    return fail(SWIT_E_ARG, "kernel_variant must be 0, 1 or 2");
+    return fail(SWIT_E_ARG, "kernel_variant must be 0, 1, 2 or 3");
   }
-  e->variant = d->kernel_variant ? d->kernel_variant : 1;
+  e->variant = d->kernel_variant ? d->kernel_variant : 3;
   if (e->variant == 2 && e->LD > 1024) {
     delete e;
     return fail(SWIT_E_LIMIT, "the fused kernels need NZ + 2 npml <= 1024 (got %d)", e->NZ);
@@ -701,6 +762,8 @@ int swit_create(const swit_desc* d, swit_engine** out) {
       delete e;
       return fail(SWIT_E_ARG, "block_x of the fused kernels must be 8, 16 or 32");
     }
+  } else if (e->variant == 3) {
+    e->bx = 0;  // one thread per 4-row vector, 256 threads per block
   } else {
     e->bx = d->block_x > 0 ? d->block_x : 4;
     if (32 * e->bx > 256 || (e->bx & (e->bx - 1))) {
@@ -708,6 +771,7 @@ int swit_create(const swit_desc* d, swit_engine** out) {
       return fail(SWIT_E_ARG, "block_x of the split kernels must be a power of two <= 8");
     }
   }
+  e->IL = e->variant == 3 ? e->L : 0;
   cudaGetDevice(&e->device);
 
   // geometry: indices exactly as fdcore.f90:70-72, 124-126, 217-218, 349-359
@@ -793,11 +857,11 @@ int swit_create(const swit_desc* d, swit_engine** out) {
   AL(valloc(e, &e->A, FSZ));
   AL(valloc(e, &e->B, FSZ));
   AL(valloc(e, &e->damp, (size_t)L + 1));
-  AL(valloc(e, &e->cint, FSI));
+  AL(valloc(e, &e->cint, e->variant == 3 ? FSZ : FSI));
   void** fields[] = {&e->p, &e->u, &e->w, &e->pb, &e->ub, &e->wb};
   for (void** f : fields) AL(valloc(e, f, (size_t)ns * FSZ));
   void** ifields[] = {&e->pe, &e->ue, &e->we, &e->dg, &e->dfw, &e->dbk};
-  for (void** f : ifields) AL(valloc(e, f, (size_t)ns * FSI));
+  for (void** f : ifields) AL(valloc(e, f, (size_t)ns * (e->variant == 3 ? FSZ : FSI)));
   if (e->variant == 2) {
     void** f2[] = {&e->p2, &e->u2, &e->w2, &e->pb2, &e->ub2, &e->wb2};
     for (void** f : f2) AL(valloc(e, f, (size_t)ns * FSZ));

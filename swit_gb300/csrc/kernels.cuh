@@ -29,6 +29,7 @@ struct Grid {
   int nx, nz, L, NX, NZ, LD, LDI, fs, fs_flag, nt, ngmax, SL;
   size_t FSZ;  // floats per PML field of one shot (NX * LD)
   size_t FSI;  // floats per interior field of one shot (nx * LDI)
+  int IL;      // interior layout offset: interior (jz, jx) at ((jx-1+IL)*LDI + jz-1+IL); npml or 0
   R dt, c1, c2;
   const R* __restrict__ A;     // den c^2 dt / dx   (fdcore.f90:79)
   const R* __restrict__ B;     // dt / (den dx)     (fdcore.f90:99)
@@ -356,7 +357,7 @@ __global__ void k_reduce(Grid<R> g, const R* __restrict__ DG, const R* __restric
   const int n = g.nx * g.nz;
   for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
     const int jx = t / g.nz, jz = t - jx * g.nz;
-    const size_t ki = (size_t)jx * g.LDI + jz;
+    const size_t ki = (size_t)(jx + g.IL) * g.LDI + (jz + g.IL);
     R a = DG[ki], b = DFW[ki], c = DBK[ki];
     for (int s = 1; s < ns; ++s) {
       a = a + DG[(size_t)s * g.FSI + ki];
@@ -471,7 +472,7 @@ __global__ void k_copy_end(Grid<R> g, const R* __restrict__ P, const R* __restri
     const int r = (int)(t - (size_t)s * g.nx * g.nz);
     const int jx = r / g.nz, jz = r - jx * g.nz;
     const size_t k = (size_t)s * g.FSZ + (size_t)(jx + g.L) * g.LD + (jz + g.L);
-    const size_t ki = (size_t)s * g.FSI + (size_t)jx * g.LDI + jz;
+    const size_t ki = (size_t)s * g.FSI + (size_t)(jx + g.IL) * g.LDI + (jz + g.IL);
     PE[ki] = P[k];
     UE[ki] = U[k];
     WE[ki] = W[k];
@@ -486,7 +487,7 @@ __global__ void k_interior_out(Grid<R> g, const R* __restrict__ F, O* out, int n
     const int s = (int)(t / ((size_t)g.nx * g.nz));
     const int r = (int)(t - (size_t)s * g.nx * g.nz);
     const int jx = r / g.nz, jz = r - jx * g.nz;
-    out[t] = (O)F[(size_t)s * g.FSI + (size_t)jx * g.LDI + jz];
+    out[t] = (O)F[(size_t)s * g.FSI + (size_t)(jx + g.IL) * g.LDI + (jz + g.IL)];
   }
 }
 

@@ -1,0 +1,534 @@
+// kernels_vec.cuh -- the split step kernels, vectorised along z.
+//
+// Each thread owns one 16-byte vector of 4 consecutive z-points of one column
+// (LD is a multiple of 32, so vectors never straddle columns).  Neighbours
+// along x are +-LD/4 vectors away, neighbours along z come from the adjacent
+// vectors of the same column.  A thread writes its own vector; the only other
+// element it may write is a free-surface mirror row (fs-1) lying in the vector
+// above its own, and the owner of that vector then leaves that one element
+// untouched -- so the in-place updates stay race-free.
+//
+// The reconstruction fields and imaging sums use the PML-grid layout of the
+// wavefields (interior point (jz, jx) at PML row jz+npml, column jx+npml), so
+// one vector covers the same rows in every array.
+//
+// Every scalar expression is the one of kernels.cuh (fdcore.f90 order, no
+// FMA): results stay bit-identical to the oracle.
+#pragma once
+#include "kernels.cuh"
+
+namespace swit {
+
+template <class R>
+struct V4 {
+  R x[4];
+};
+
+template <class R>
+__device__ __forceinline__ V4<R> ld4(const R* p, size_t k4) {
+  V4<R> v;
+  if constexpr (sizeof(R) == 4) {
+    const float4 t = reinterpret_cast<const float4*>(p)[k4];
+    v.x[0] = t.x;
+    v.x[1] = t.y;
+    v.x[2] = t.z;
+    v.x[3] = t.w;
+  } else {
+    const double2 a = reinterpret_cast<const double2*>(p)[2 * k4];
+    const double2 b = reinterpret_cast<const double2*>(p)[2 * k4 + 1];
+    v.x[0] = a.x;
+    v.x[1] = a.y;
+    v.x[2] = b.x;
+    v.x[3] = b.y;
+  }
+  return v;
+}
+
+template <class R>
+__device__ __forceinline__ void st4(R* p, size_t k4, const V4<R>& v) {
+  if constexpr (sizeof(R) == 4) {
+    reinterpret_cast<float4*>(p)[k4] = make_float4(v.x[0], v.x[1], v.x[2], v.x[3]);
+  } else {
+    reinterpret_cast<double2*>(p)[2 * k4] = make_double2(v.x[0], v.x[1]);
+    reinterpret_cast<double2*>(p)[2 * k4 + 1] = make_double2(v.x[2], v.x[3]);
+  }
+}
+
+// Stores the vector except element `skip` (the mirror row another thread writes).
+template <class R>
+__device__ __forceinline__ void st4_except(R* p, size_t k4, const V4<R>& v, int skip) {
+#pragma unroll
+  for (int j = 0; j < 4; ++j)
+    if (j != skip) p[4 * k4 + j] = v.x[j];
+}
+
+// Damping at (iz, ix), zero without any test in the interior block.
+template <class R>
+__device__ __forceinline__ R dampv(const Grid<R>& g, int iz, int ix) {
+  if (ix > g.L && ix <= g.NX - g.L && iz > g.L && iz <= g.NZ - g.L) return R(0);
+  return damp_at(g.damp, iz, ix, g.L, g.NX, g.NZ);
+}
+
+// Thread -> (shot, column, first row) of its vector.
+struct VecIdx {
+  int s, ix, iz0, q;
+  size_t k4;  // vector index within the shot
+  bool ok;
+};
+template <class R>
+__device__ __forceinline__ VecIdx vec_index(const Grid<R>& g, int shot0) {
+  VecIdx v;
+  const int LD4 = g.LD >> 2;
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  v.s = shot0 + blockIdx.y;
+  v.ok = t < g.NX * LD4;
+  v.ix = t / LD4 + 1;
+  v.q = t - (v.ix - 1) * LD4;
+  v.iz0 = 4 * v.q + 1;
+  v.k4 = (size_t)t;
+  return v;
+}
+
+// ---------------------------------------------------------------------------
+// Forward pressure phase (fdcore.f90:77-94).
+template <class R>
+__global__ void __launch_bounds__(256) k_fwd_p_v(Grid<R> g, Sources src, const R* __restrict__ s_fwd, R* P,
+                                                 const R* __restrict__ U, const R* __restrict__ W, int it, int shot0) {
+  const VecIdx v = vec_index(g, shot0);
+  if (!v.ok) return;
+  const int LD4 = g.LD >> 2, ix = v.ix, iz0 = v.iz0, fs = g.fs, NZ = g.NZ;
+  const size_t off = (size_t)v.s * g.FSZ;
+  R* p = P + off;
+  const R* u = U + off;
+  const R* w = W + off;
+  V4<R> pv = ld4(p, v.k4);
+  bool dirty = false;
+  if (ix >= 3 && ix <= g.NX - 2 && iz0 + 3 >= fs + 1 && iz0 <= NZ - 2) {
+    const V4<R> a = ld4(g.A, v.k4);
+    const V4<R> u0 = ld4(u, v.k4), um1 = ld4(u, v.k4 - LD4), up1 = ld4(u, v.k4 + LD4), um2 = ld4(u, v.k4 - 2 * LD4);
+    R wz[7];  // w at rows iz0-2 .. iz0+4
+    const V4<R> w0 = ld4(w, v.k4);
+    wz[2] = w0.x[0];
+    wz[3] = w0.x[1];
+    wz[4] = w0.x[2];
+    wz[5] = w0.x[3];
+    if (v.q > 0) {
+      const V4<R> wm = ld4(w, v.k4 - 1);
+      wz[0] = wm.x[2];
+      wz[1] = wm.x[3];
+    } else {
+      wz[0] = wz[1] = R(0);
+    }
+    wz[6] = (v.q + 1 < LD4) ? w[(size_t)ix * g.LD - g.LD + iz0 + 3] : R(0);
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const int iz = iz0 + j;
+      if (iz >= fs + 1 && iz <= NZ - 2) {
+        const R kappa = dampv(g, iz, ix) * g.dt;
+        pv.x[j] = (R(1.0) - kappa) * pv.x[j] -
+                  a.x[j] * (g.c1 * (u0.x[j] - um1.x[j] + wz[j + 2] - wz[j + 1]) +
+                            g.c2 * (up1.x[j] - um2.x[j] + wz[j + 3] - wz[j]));
+      }
+    }
+    dirty = true;
+  }
+  const int js = src.isz[v.s] - iz0;
+  if (ix == src.isx[v.s] && js >= 0 && js < 4) {
+    pv.x[js] = pv.x[js] + g.dt * s_fwd[(size_t)v.s * (g.nt + 1) + (it - 1)];
+    dirty = true;
+  }
+  // p(fs-1, :) = -p(fs+1, :) (fdcore.f90:92-94).  Rows fs-1 and fs+1 share a
+  // vector, or row fs-1 is in the vector above, whose rows (<= fs) this phase
+  // never changes: its owner stores nothing and the owner of fs+1 writes it.
+  const int jm = fs - 1 - iz0, jp = fs + 1 - iz0;
+  if (g.fs_flag == 1 && jp >= 0 && jp < 4) {
+    if (jm >= 0) {
+      pv.x[jm] = -pv.x[jp];
+      dirty = true;
+    } else {
+      p[(size_t)(ix - 1) * g.LD + (fs - 2)] = -pv.x[jp];
+    }
+  }
+  if (dirty) st4(p, v.k4, pv);
+}
+
+// Forward velocity phase (fdcore.f90:97-159).
+template <class R>
+__global__ void __launch_bounds__(256) k_fwd_uw_v(Grid<R> g, Receivers rec, const R* __restrict__ P, R* U, R* W,
+                                                  R* __restrict__ seis_t, R* __restrict__ strips, int it, int shot0) {
+  const VecIdx v = vec_index(g, shot0);
+  if (!v.ok) return;
+  const int LD4 = g.LD >> 2, ix = v.ix, iz0 = v.iz0, fs = g.fs, NZ = g.NZ, NX = g.NX, L = g.L;
+  const size_t off = (size_t)v.s * g.FSZ;
+  const R* p = P + off;
+  R* u = U + off;
+  R* w = W + off;
+  const V4<R> p0 = ld4(p, v.k4);
+  V4<R> uv = ld4(u, v.k4), wv = ld4(w, v.k4);
+  bool du = false, dw = false;
+  const bool rows = iz0 + 3 >= fs && iz0 <= NZ - 1;
+  if (rows && ix >= 2 && ix <= NX - 1) {
+    const V4<R> b = ld4(g.B, v.k4);
+    if (ix <= NX - 2) {
+      const V4<R> pp1 = ld4(p, v.k4 + LD4), pp2 = ld4(p, v.k4 + 2 * LD4), pm1 = ld4(p, v.k4 - LD4);
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const int iz = iz0 + j;
+        if (iz >= fs && iz <= NZ - 1) {
+          const R kappa = R(0.5) * (dampv(g, iz, ix) + dampv(g, iz, ix + 1)) * g.dt;
+          uv.x[j] = (R(1.0) - kappa) * uv.x[j] - b.x[j] * (g.c1 * (pp1.x[j] - p0.x[j]) + g.c2 * (pp2.x[j] - pm1.x[j]));
+        }
+      }
+      du = true;
+    }
+    R pz[7];  // p at rows iz0-1 .. iz0+5
+    pz[1] = p0.x[0];
+    pz[2] = p0.x[1];
+    pz[3] = p0.x[2];
+    pz[4] = p0.x[3];
+    pz[0] = v.q > 0 ? p[(size_t)(ix - 1) * g.LD + iz0 - 2] : R(0);
+    if (v.q + 1 < LD4) {
+      const V4<R> pn = ld4(p, v.k4 + 1);
+      pz[5] = pn.x[0];
+      pz[6] = pn.x[1];
+    } else {
+      pz[5] = pz[6] = R(0);
+    }
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const int iz = iz0 + j;
+      if (iz >= fs && iz <= NZ - 2) {
+        const R kappa = R(0.5) * (dampv(g, iz, ix) + dampv(g, iz + 1, ix)) * g.dt;
+        wv.x[j] = (R(1.0) - kappa) * wv.x[j] - b.x[j] * (g.c1 * (pz[j + 2] - pz[j + 1]) + g.c2 * (pz[j + 3] - pz[j]));
+      }
+    }
+    dw = true;
+  }
+  // w(fs-1, ix) = w(fs, ix) for every column (fdcore.f90:116-120).  If row
+  // fs-1 ends the vector above, that vector (rows < fs) has no u or w update
+  // and its owner stores nothing; the owner of row fs writes the mirror.
+  const int jm = fs - 1 - iz0, jr = fs - iz0;
+  if (g.fs_flag == 1 && jr >= 0 && jr < 4) {
+    if (jm >= 0) {
+      wv.x[jm] = wv.x[jr];
+      dw = true;
+    } else {
+      w[(size_t)(ix - 1) * g.LD + (fs - 2)] = wv.x[jr];
+    }
+  }
+  if (du) st4(u, v.k4, uv);
+  if (dw) st4(w, v.k4, wv);
+  // receivers (fdcore.f90:123-128)
+  {
+    const int* cp = rec.colptr + (size_t)v.s * (NX + 2);
+    const int e1 = cp[ix + 1];
+    for (int e = cp[ix]; e < e1; ++e) {
+      const int j = rec.zrow[e] - iz0;
+      if (j >= 0 && j < 4) seis_t[((size_t)v.s * g.nt + (it - 1)) * g.ngmax + rec.ig[e]] = p0.x[j];
+    }
+  }
+  if (strips) {
+    R* b = strips + ((size_t)v.s * g.nt + (it - 1)) * g.SL;
+    const StripOff o = strip_offsets(g.nx, g.nz);
+    const int jx = ix - L;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const int iz = iz0 + j, jz = iz - L;
+      if (jx >= 1 && jx <= g.nx) {
+        if (iz == NZ - L) b[o.B0 + jx - 1] = p0.x[j];
+        if (iz == NZ - L - 1) {
+          b[o.B1 + jx - 1] = p0.x[j];
+          b[o.B2 + jx - 1] = wv.x[j];
+        }
+        if (iz == fs) {
+          b[o.T0 + jx - 1] = p0.x[j];
+          b[o.T3 + jx - 1] = uv.x[j];
+          b[o.T5 + jx - 1] = wv.x[j];
+        }
+        if (iz == fs + 1) {
+          b[o.T1 + jx - 1] = p0.x[j];
+          b[o.T4 + jx - 1] = uv.x[j];
+        }
+        if (iz == fs + 2) b[o.T2 + jx - 1] = p0.x[j];
+      }
+      if (jz >= 1 && jz <= g.nz) {
+        if (ix == L + 1) {
+          b[o.S0 + jz - 1] = p0.x[j];
+          b[o.S2 + jz - 1] = uv.x[j];
+        }
+        if (ix == L + 2) b[o.S1 + jz - 1] = p0.x[j];
+        if (ix == NX - L) b[o.S3 + jz - 1] = p0.x[j];
+        if (ix == NX - L - 1) {
+          b[o.S4 + jz - 1] = p0.x[j];
+          b[o.S5 + jz - 1] = uv.x[j];
+        }
+      }
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Backward velocity phase: adjoint u, w (fdcore.f90:309-333) and the
+// reconstruction u, w with their re-insert (fdcore.f90:220-247).
+template <class R>
+__global__ void __launch_bounds__(256) k_bwd_uw_v(Grid<R> g, const R* __restrict__ PB, R* UB, R* WB,
+                                                  const R* __restrict__ PE, R* UE, R* WE,
+                                                  const R* __restrict__ strips, int it, int shot0) {
+  const VecIdx v = vec_index(g, shot0);
+  if (!v.ok) return;
+  const int LD4 = g.LD >> 2, ix = v.ix, iz0 = v.iz0, fs = g.fs, NZ = g.NZ, NX = g.NX, L = g.L;
+  const size_t off = (size_t)v.s * g.FSZ;
+  const R* pb = PB + off;
+  R* ub = UB + off;
+  R* wb = WB + off;
+  // ---- adjoint: u on ix in [2, NX-2], iz in [2, NZ-1]; w on ix in [2, NX-1], iz in [2, NZ-2]
+  if (ix >= 2 && ix <= NX - 1 && iz0 <= NZ - 1) {
+    const V4<R> a = ld4(g.A, v.k4);
+    const V4<R> p0 = ld4(pb, v.k4);
+    if (ix <= NX - 2) {
+      V4<R> uv = ld4(ub, v.k4);
+      const V4<R> pp1 = ld4(pb, v.k4 + LD4), pp2 = ld4(pb, v.k4 + 2 * LD4), pm1 = ld4(pb, v.k4 - LD4);
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const int iz = iz0 + j;
+        if (iz >= 2 && iz <= NZ - 1) {
+          const R kappa = R(0.5) * (dampv(g, iz, ix) + dampv(g, iz, ix + 1)) * g.dt;
+          uv.x[j] = (R(1.0) - kappa) * uv.x[j] - a.x[j] * (g.c1 * (pp1.x[j] - p0.x[j]) + g.c2 * (pp2.x[j] - pm1.x[j]));
+        }
+      }
+      st4(ub, v.k4, uv);
+    }
+    V4<R> wv = ld4(wb, v.k4);
+    R pz[7];  // pb at rows iz0-1 .. iz0+5
+    pz[1] = p0.x[0];
+    pz[2] = p0.x[1];
+    pz[3] = p0.x[2];
+    pz[4] = p0.x[3];
+    pz[0] = v.q > 0 ? pb[(size_t)(ix - 1) * g.LD + iz0 - 2] : R(0);
+    if (v.q + 1 < LD4) {
+      const V4<R> pn = ld4(pb, v.k4 + 1);
+      pz[5] = pn.x[0];
+      pz[6] = pn.x[1];
+    } else {
+      pz[5] = pz[6] = R(0);
+    }
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const int iz = iz0 + j;
+      if (iz >= 2 && iz <= NZ - 2) {
+        const R kappa = R(0.5) * (dampv(g, iz, ix) + dampv(g, iz + 1, ix)) * g.dt;
+        wv.x[j] = (R(1.0) - kappa) * wv.x[j] - a.x[j] * (g.c1 * (pz[j + 2] - pz[j + 1]) + g.c2 * (pz[j + 3] - pz[j]));
+      }
+    }
+    // w(fs-1, ix) = w(fs, ix) for ix in [2, NX-1] (fdcore.f90:329-333).  When
+    // row fs-1 ends the vector above, the owner of row fs writes it and that
+    // vector's owner stores its other three rows.
+    const int jm = fs - 1 - iz0, jr = fs - iz0;
+    if (g.fs_flag == 1 && jr == 0) wb[(size_t)(ix - 1) * g.LD + (fs - 2)] = wv.x[0];
+    if (g.fs_flag == 1 && jm >= 0 && jm < 4) {
+      if (jr < 4) {
+        wv.x[jm] = wv.x[jr];
+        st4(wb, v.k4, wv);
+      } else {
+        st4_except(wb, v.k4, wv, jm);
+      }
+    } else {
+      st4(wb, v.k4, wv);
+    }
+  }
+  // ---- reconstruction on the interior
+  const int jx = ix - L, jz0 = iz0 - L;
+  if (jx < 1 || jx > g.nx || jz0 + 3 < 1 || jz0 > g.nz) return;
+  const int nx = g.nx, nz = g.nz, fsi = fs - L;
+  const R* pe = PE + off;
+  R* ue = UE + off;
+  R* we = WE + off;
+  const R* b = strips + ((size_t)v.s * g.nt + (it - 2)) * g.SL;  // boundary(:, it-1)
+  const StripOff o = strip_offsets(nx, nz);
+  const V4<R> bb = ld4(g.B, v.k4);
+  const V4<R> e0 = ld4(pe, v.k4);
+  V4<R> uv = ld4(ue, v.k4), wv = ld4(we, v.k4);
+  if (jx >= 2 && jx <= nx - 2) {
+    const V4<R> ep1 = ld4(pe, v.k4 + LD4), ep2 = ld4(pe, v.k4 + 2 * LD4), em1 = ld4(pe, v.k4 - LD4);
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const int jz = jz0 + j;
+      if (jz >= fsi + 1 && jz <= nz - 1)
+        uv.x[j] = uv.x[j] + bb.x[j] * (g.c1 * (ep1.x[j] - e0.x[j]) + g.c2 * (ep2.x[j] - em1.x[j]));
+    }
+  }
+  if (jx >= 2 && jx <= nx - 1) {
+    R ez[7];  // pe at rows iz0-1 .. iz0+5 (zero outside the interior)
+    ez[1] = e0.x[0];
+    ez[2] = e0.x[1];
+    ez[3] = e0.x[2];
+    ez[4] = e0.x[3];
+    ez[0] = v.q > 0 ? pe[(size_t)(ix - 1) * g.LD + iz0 - 2] : R(0);
+    if (v.q + 1 < LD4) {
+      const V4<R> en = ld4(pe, v.k4 + 1);
+      ez[5] = en.x[0];
+      ez[6] = en.x[1];
+    } else {
+      ez[5] = ez[6] = R(0);
+    }
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const int jz = jz0 + j;
+      if (jz >= fsi + 1 && jz <= nz - 2)
+        wv.x[j] = wv.x[j] + bb.x[j] * (g.c1 * (ez[j + 2] - ez[j + 1]) + g.c2 * (ez[j + 3] - ez[j]));
+    }
+  }
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    const int jz = jz0 + j;
+    if (jz < 1 || jz > nz) continue;
+    if (jz == nz - 1) wv.x[j] = b[o.B2 + jx - 1];
+    if (jx == 1) uv.x[j] = b[o.S2 + jz - 1];
+    if (jx == nx - 1) uv.x[j] = b[o.S5 + jz - 1];
+  }
+  st4(ue, v.k4, uv);
+  st4(we, v.k4, wv);
+}
+
+// Backward pressure phase: adjoint p + injection + mirror (fdcore.f90:336-373),
+// reconstruction p with source subtraction and re-insert (fdcore.f90:249-287),
+// imaging sums (solver.f90:237-239).
+template <class R>
+__global__ void __launch_bounds__(256) k_bwd_p_v(Grid<R> g, Receivers rec, Sources src, const R* __restrict__ s_fwd,
+                                                 const R* __restrict__ adj_t, R* PB, const R* __restrict__ UB,
+                                                 const R* __restrict__ WB, R* PE, const R* __restrict__ UE,
+                                                 const R* __restrict__ WE, R* DG, R* DFW, R* DBK,
+                                                 const R* __restrict__ strips, int it, int shot0) {
+  const VecIdx v = vec_index(g, shot0);
+  if (!v.ok) return;
+  const int LD4 = g.LD >> 2, ix = v.ix, iz0 = v.iz0, fs = g.fs, NZ = g.NZ, NX = g.NX, L = g.L;
+  const size_t off = (size_t)v.s * g.FSZ;
+  R* pb = PB + off;
+  const R* ub = UB + off;
+  const R* wb = WB + off;
+  const V4<R> pold = ld4(pb, v.k4);
+  V4<R> pv = pold;
+  bool dirty = false;
+  if (ix >= 3 && ix <= NX - 2 && iz0 + 3 >= 3 && iz0 <= NZ - 2) {
+    const V4<R> bcoef = ld4(g.B, v.k4);
+    const V4<R> u0 = ld4(ub, v.k4), um1 = ld4(ub, v.k4 - LD4), up1 = ld4(ub, v.k4 + LD4), um2 = ld4(ub, v.k4 - 2 * LD4);
+    R wz[7];  // wb at rows iz0-2 .. iz0+4
+    const V4<R> w0 = ld4(wb, v.k4);
+    wz[2] = w0.x[0];
+    wz[3] = w0.x[1];
+    wz[4] = w0.x[2];
+    wz[5] = w0.x[3];
+    if (v.q > 0) {
+      const V4<R> wm = ld4(wb, v.k4 - 1);
+      wz[0] = wm.x[2];
+      wz[1] = wm.x[3];
+    } else {
+      wz[0] = wz[1] = R(0);
+    }
+    wz[6] = (v.q + 1 < LD4) ? wb[(size_t)(ix - 1) * g.LD + iz0 + 3] : R(0);
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const int iz = iz0 + j;
+      if (iz >= 3 && iz <= NZ - 2) {
+        const R kappa = dampv(g, iz, ix) * g.dt;
+        pv.x[j] = (R(1.0) - kappa) * pv.x[j] -
+                  bcoef.x[j] * (g.c1 * (u0.x[j] - um1.x[j] + wz[j + 2] - wz[j + 1]) +
+                                g.c2 * (up1.x[j] - um2.x[j] + wz[j + 3] - wz[j]));
+      }
+    }
+    dirty = true;
+  }
+  {
+    const int* cp = rec.colptr + (size_t)v.s * (NX + 2);
+    const int e1 = cp[ix + 1];
+    for (int e = cp[ix]; e < e1; ++e) {
+      const int j = rec.zrow[e] - iz0;
+      if (j >= 0 && j < 4) {
+        pv.x[j] = pv.x[j] + g.dt * adj_t[((size_t)v.s * g.nt + (it - 1)) * g.ngmax + rec.ig[e]];
+        dirty = true;
+      }
+    }
+  }
+  // p(fs-1, ix) = -p(fs+1, ix) for every column (fdcore.f90:370-373).  When
+  // row fs-1 lies in the vector above, the owner of row fs+1 writes it and
+  // that vector's owner stores its other rows.
+  const int jm = fs - 1 - iz0, jp = fs + 1 - iz0;
+  if (jp >= 0 && jp < 4 && jm < 0) pb[(size_t)(ix - 1) * g.LD + (fs - 2)] = -pv.x[jp];
+  if (jm >= 0 && jm < 4) {
+    if (jp < 4) {
+      pv.x[jm] = -pv.x[jp];
+      st4(pb, v.k4, pv);
+    } else {
+      st4_except(pb, v.k4, pv, jm);
+    }
+  } else if (dirty) {
+    st4(pb, v.k4, pv);
+  }
+
+  // ---- reconstruction p, re-insert, imaging on the interior
+  const int jx = ix - L, jz0 = iz0 - L;
+  if (jx < 1 || jx > g.nx || jz0 + 3 < 1 || jz0 > g.nz) return;
+  const int nx = g.nx, nz = g.nz, fsi = fs - L;
+  R* pe = PE + off;
+  const R* ue = UE + off;
+  const R* we = WE + off;
+  const R* b = strips + ((size_t)v.s * g.nt + (it - 2)) * g.SL;
+  const StripOff o = strip_offsets(nx, nz);
+  V4<R> ev = ld4(pe, v.k4);
+  const int rj = src.risz[v.s] - jz0;
+  if (jx == src.risx[v.s] && rj >= 0 && rj < 4) ev.x[rj] = ev.x[rj] - g.dt * s_fwd[(size_t)v.s * (g.nt + 1) + it];
+  if (jx >= 3 && jx <= nx - 2) {
+    const V4<R> a = ld4(g.A, v.k4);
+    const V4<R> u0 = ld4(ue, v.k4), um1 = ld4(ue, v.k4 - LD4), up1 = ld4(ue, v.k4 + LD4), um2 = ld4(ue, v.k4 - 2 * LD4);
+    R wz[7];
+    const V4<R> w0 = ld4(we, v.k4);
+    wz[2] = w0.x[0];
+    wz[3] = w0.x[1];
+    wz[4] = w0.x[2];
+    wz[5] = w0.x[3];
+    if (v.q > 0) {
+      const V4<R> wm = ld4(we, v.k4 - 1);
+      wz[0] = wm.x[2];
+      wz[1] = wm.x[3];
+    } else {
+      wz[0] = wz[1] = R(0);
+    }
+    wz[6] = (v.q + 1 < LD4) ? we[(size_t)(ix - 1) * g.LD + iz0 + 3] : R(0);
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const int jz = jz0 + j;
+      if (jz >= fsi + 2 && jz <= nz - 2)
+        ev.x[j] = ev.x[j] + a.x[j] * (g.c1 * (u0.x[j] - um1.x[j] + wz[j + 2] - wz[j + 1]) +
+                                      g.c2 * (up1.x[j] - um2.x[j] + wz[j + 3] - wz[j]));
+    }
+  }
+  R* dg = DG + off;
+  R* dfw = DFW + off;
+  R* dbk = DBK + off;
+  V4<R> g0 = ld4(dg, v.k4), f0 = ld4(dfw, v.k4), k0 = ld4(dbk, v.k4);
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    const int jz = jz0 + j;
+    if (jz < 1 || jz > nz) continue;
+    R pf = ev.x[j];
+    if (jz == nz) pf = b[o.B0 + jx - 1];
+    if (jz == nz - 1) pf = b[o.B1 + jx - 1];
+    if (jx == 1) pf = b[o.S0 + jz - 1];
+    if (jx == 2) pf = b[o.S1 + jz - 1];
+    if (jx == nx) pf = b[o.S3 + jz - 1];
+    if (jx == nx - 1) pf = b[o.S4 + jz - 1];
+    if (jz == fsi) pf = b[o.T0 + jx - 1];
+    if (jz == fsi + 1) pf = b[o.T1 + jx - 1];
+    if (jz == fsi + 2) pf = b[o.T2 + jx - 1];
+    ev.x[j] = pf;
+    g0.x[j] = g0.x[j] + pf * (pold.x[j] - pv.x[j]);
+    f0.x[j] = f0.x[j] + pf * pf;
+    k0.x[j] = k0.x[j] + pv.x[j] * pv.x[j];
+  }
+  st4(pe, v.k4, ev);
+  st4(dg, v.k4, g0);
+  st4(dfw, v.k4, f0);
+  st4(dbk, v.k4, k0);
+}
+
+}  // namespace swit

@@ -265,6 +265,7 @@ extern "C" int swit_forward_shot_static(int32_t nx, int32_t nz, int32_t npml, in
   g.SL = 0;
   g.FSZ = 0;  // one shot
   g.FSI = 0;
+  g.IL = 0;
   g.dt = dt;
   g.c1 = 9.0f / 8.0f;
   g.c2 = -1.0f / 24.0f;

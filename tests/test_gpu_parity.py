@@ -56,9 +56,10 @@ def test_forward_seismograms_match_oracle(base):
     np.testing.assert_array_equal(seis, base["ref"]["seis"])
 
 
-def test_boundary_strips_and_end_states_match_oracle(base):
+@pytest.mark.parametrize("kernel", ["split", "vec"])
+def test_boundary_strips_and_end_states_match_oracle(base, kernel):
     s = base["s"]
-    with engine(s) as e:
+    with engine(s, kernel=kernel) as e:
         e.set_model(s.vp_true, base["rho"])
         e.forward(base["src"], save_boundary=True)
         snap = e.export_snapshot()
@@ -96,7 +97,8 @@ def test_gradient_l2_single_call_matches_oracle(base):
                                   dict(kernel="fused", block_x=32), dict(kernel="fused", path="plain"),
                                   dict(kernel="split"), dict(kernel="split", block_x=8),
                                   dict(kernel="split", block_x=1), dict(kernel="split", path="plain"),
-                                  dict(kernel="split", shots_per_batch=2)])
+                                  dict(kernel="split", shots_per_batch=2), dict(kernel="vec"),
+                                  dict(kernel="vec", path="plain"), dict(kernel="vec", shots_per_batch=2)])
 def test_launch_variants_are_identical(base, opts):
     s = base["s"]
     with engine(s, **opts) as e:
@@ -108,7 +110,7 @@ def test_launch_variants_are_identical(base, opts):
     np.testing.assert_array_equal(bk, base["grad"]["bk"])
 
 
-@pytest.mark.parametrize("kernel", ["fused", "split"])
+@pytest.mark.parametrize("kernel", ["fused", "split", "vec"])
 def test_fp64_build_matches_fp64_oracle(base, kernel):
     s, pb = base["s"], base["pb"]
     ref = O.forward(pb, s.vp_true, base["rho"], base["src"], store=True, fp64=True)
@@ -133,7 +135,7 @@ def test_repeated_backward_after_one_forward(base):
     np.testing.assert_array_equal(g2, base["grad"]["g"])
 
 
-@pytest.mark.parametrize("kernel", ["fused", "split"])
+@pytest.mark.parametrize("kernel", ["fused", "split", "vec"])
 def test_edge_geometry_surface_receivers_deep_source_uneven_traces(kernel):
     """Receivers on z = 0 (moved one node down), a source deep enough that the
     reconstruction subtracts it (fdcore.f90:250-256), shots with different
@@ -161,7 +163,7 @@ def test_edge_geometry_surface_receivers_deep_source_uneven_traces(kernel):
     np.testing.assert_array_equal(bk, gref["bk"])
 
 
-@pytest.mark.parametrize("kernel", ["fused", "split"])
+@pytest.mark.parametrize("kernel", ["fused", "split", "vec"])
 def test_no_free_surface(kernel):
     s, _ = case(nt=200)
     s.free_surface = 0
@@ -208,3 +210,24 @@ def test_state_and_model_errors(base):
         e.set_model(s.vp_true, base["rho"])
         with pytest.raises(SwitError, match="SWIT_E_STATE"):
             e.backward(base["adj"])
+
+
+@pytest.mark.parametrize("npml", [8, 9, 10, 11])
+def test_vec_kernels_every_mirror_alignment(npml):
+    """The vectorised kernels own 4 rows per thread; npml mod 4 decides whether
+    the free-surface mirror rows fs-1 and fs / fs+1 share a vector or not."""
+    s = survey.small(nx=36, nz=28, npml=npml, nt=160, ns=2, zs=70.0, zr=0.0)
+    pb = O.Problem(s.nx, s.nz, s.npml, s.nt, s.dx, s.dt, s.src_xz, s.rec_xz)
+    src = s.source()
+    rho = s.rho(s.vp_true)
+    ref = O.forward(pb, s.vp_true, rho, src, store=True)
+    adj = np.random.default_rng(npml).standard_normal(ref["seis"].shape).astype(np.float32)
+    gref = O.adjoint(pb, s.vp_true, rho, src, adj, ref)
+    with engine(s, kernel="vec") as e:
+        e.set_model(s.vp_true, rho)
+        seis = e.forward(src, save_boundary=True)
+        g, fw, bk = e.backward(adj)
+    np.testing.assert_array_equal(seis, ref["seis"])
+    np.testing.assert_array_equal(g, gref["g"])
+    np.testing.assert_array_equal(fw, gref["fw"])
+    np.testing.assert_array_equal(bk, gref["bk"])
