@@ -37,14 +37,16 @@ def _desc(s, **over):
     keep = [ng, xs, zs, xg, zg]
     f = dict(nx=s.nx, nz=s.nz, npml=s.npml, nt=s.nt, dx=s.dx, dt=s.dt, free_surface=1, ns=s.ns, ng_max=s.ng,
              ng=ng.ctypes.data, src_x=xs.ctypes.data, src_z=zs.ctypes.data, rec_x=xg.ctypes.data,
-             rec_z=zg.ctypes.data, precision=0, path=0, shots_per_batch=0, block_x=0)
+             rec_z=zg.ctypes.data, precision=0, path=0, shots_per_batch=0, block_x=0, kernel_variant=0)
     f.update(over)
     return _lib.SwitDesc(**f), keep
 
 
 @pytest.mark.parametrize("over,code", [
     (dict(nx=4), _lib.SwitError), (dict(npml=1), _lib.SwitError), (dict(nt=1), _lib.SwitError),
-    (dict(dx=0.0), _lib.SwitError), (dict(precision=3), _lib.SwitError), (dict(block_x=3), _lib.SwitError),
+    (dict(dx=0.0), _lib.SwitError), (dict(precision=3), _lib.SwitError),
+    (dict(block_x=3, kernel_variant=1), _lib.SwitError), (dict(block_x=12, kernel_variant=2), _lib.SwitError),
+    (dict(kernel_variant=7), _lib.SwitError),
 ])
 def test_create_rejects_bad_descriptions_before_any_gpu_work(over, code):
     lib = _lib.load()
