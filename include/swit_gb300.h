@@ -71,7 +71,8 @@ typedef struct swit_desc {
   int32_t shots_per_batch;  /* batched path: shots per launch, 0 = automatic    */
   int32_t block_x;          /* columns per CTA, 0 = automatic: split kernels
                                1, 2, 4 or 8 (x 32 rows); fused kernels 8, 16
-                               or 32 (x all rows); ignored by vec                */
+                               or 32 (x all rows); vec kernels 4..64 columns x
+                               256/block_x four-row vectors (default 32)         */
   int32_t kernel_variant;   /* 0 = automatic (vec), 1 = split: two kernels per step,
                                in place, one point per thread; 2 = fused: one
                                kernel per step, double-buffered (NZ + 2 npml <=

@@ -25,8 +25,9 @@ def candidates(ns, nz_pml):
         for tx in (8, 16, 32):
             for b in batches:
                 out.append(dict(kernel="fused", block_x=tx, shots_per_batch=b))
-    for b in batches:
-        out.append(dict(kernel="vec", shots_per_batch=b))
+    for bx in (8, 16, 32):
+        for b in batches:
+            out.append(dict(kernel="vec", block_x=bx, shots_per_batch=b))
     out.append(dict(kernel="split", block_x=4, shots_per_batch=ns))
     return out
 

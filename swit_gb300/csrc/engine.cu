@@ -59,10 +59,10 @@ struct swit_engine {
   int IL;       // interior fields: row/column offset into their layout (npml for vec, else 0)
   int device;
   size_t esz;  // sizeof(R)
-  std::vector<int> ng, isx, isz, risx, risz, colptr, ent_ig, ent_zr;
+  std::vector<int> ng, isx, isz, risx, risz, colptr, ent_ig, ent_zr, zlo, zhi;
   // device tables
   int *d_ng = nullptr, *d_isx = nullptr, *d_isz = nullptr, *d_risx = nullptr, *d_risz = nullptr;
-  int *d_colptr = nullptr, *d_ig = nullptr, *d_zr = nullptr, *d_live = nullptr;
+  int *d_colptr = nullptr, *d_ig = nullptr, *d_zr = nullptr, *d_live = nullptr, *d_zlo = nullptr, *d_zhi = nullptr;
   double* d_mtrace = nullptr;
   // device arrays of type R (float or double)
   void *A = nullptr, *B = nullptr, *damp = nullptr, *cint = nullptr;
@@ -112,7 +112,7 @@ void release(swit_engine* e) {
     if (e->gfwd[i]) cudaGraphExecDestroy(e->gfwd[i]);
   if (e->gbwd) cudaGraphExecDestroy(e->gbwd);
   if (e->cap) cudaStreamDestroy(e->cap);
-  void* ptrs[] = {e->d_ng, e->d_isx, e->d_isz, e->d_risx, e->d_risz, e->d_colptr, e->d_ig, e->d_zr, e->d_live,
+  void* ptrs[] = {e->d_zlo, e->d_zhi, e->d_ng, e->d_isx, e->d_isz, e->d_risx, e->d_risz, e->d_colptr, e->d_ig, e->d_zr, e->d_live,
                   e->d_mtrace, e->A, e->B, e->damp, e->cint, e->p, e->u, e->w, e->pb, e->ub, e->wb, e->pe,
                   e->ue, e->we, e->dg, e->dfw, e->dbk, e->strips, e->src, e->seis_t, e->adj_t, e->d_in,
                   e->d_stage, e->p2, e->u2, e->w2, e->pb2, e->ub2, e->wb2, e->pe2, e->ue2, e->we2};
@@ -148,7 +148,9 @@ Grid<R> make_grid(const swit_engine* e) {
   return g;
 }
 
-inline Receivers make_rec(const swit_engine* e) { return Receivers{e->d_colptr, e->d_ig, e->d_zr}; }
+inline Receivers make_rec(const swit_engine* e) {
+  return Receivers{e->d_colptr, e->d_ig, e->d_zr, e->d_zlo, e->d_zhi};
+}
 inline Sources make_src(const swit_engine* e) { return Sources{e->d_isx, e->d_isz, e->d_risx, e->d_risz}; }
 
 // Launch shape of the stencil kernels for a batch of nb shots.
@@ -215,8 +217,11 @@ void launch_bwd_step(swit_engine* e, int shot0, int nb, int it, cudaStream_t st)
 #undef BWD
 }
 
+// Tiles of (256 / block_x) vectors along z by block_x columns.
+inline dim3 vec_block(const swit_engine* e) { return dim3(256 / e->bx, e->bx); }
 inline dim3 vec_grid(const swit_engine* e, int nb) {
-  return dim3((unsigned)(((size_t)e->NX * (e->LD / 4) + 255) / 256), nb);
+  const int vz = 256 / e->bx;
+  return dim3((e->LD / 4 + vz - 1) / vz, (e->NX + e->bx - 1) / e->bx, nb);
 }
 
 // Forward time loop of shots [shot0, shot0+nb): fdcore.f90:75-160.
@@ -227,9 +232,9 @@ void launch_forward_steps(swit_engine* e, bool store, int shot0, int nb, cudaStr
     R* strips = store ? (R*)e->strips : nullptr;
     const dim3 grid = vec_grid(e, nb);
     for (int it = 2; it <= e->nt; ++it) {
-      k_fwd_p_v<R><<<grid, 256, 0, st>>>(g, make_src(e), (const R*)e->src, (R*)e->p, (const R*)e->u, (const R*)e->w,
+      k_fwd_p_v<R><<<grid, vec_block(e), 0, st>>>(g, make_src(e), (const R*)e->src, (R*)e->p, (const R*)e->u, (const R*)e->w,
                                          it, shot0);
-      k_fwd_uw_v<R><<<grid, 256, 0, st>>>(g, make_rec(e), (const R*)e->p, (R*)e->u, (R*)e->w, (R*)e->seis_t, strips,
+      k_fwd_uw_v<R><<<grid, vec_block(e), 0, st>>>(g, make_rec(e), (const R*)e->p, (R*)e->u, (R*)e->w, (R*)e->seis_t, strips,
                                           it, shot0);
     }
     return;
@@ -257,9 +262,9 @@ void launch_backward_steps(swit_engine* e, int shot0, int nb, cudaStream_t st) {
     Grid<R> g = make_grid<R>(e);
     const dim3 grid = vec_grid(e, nb);
     for (int it = e->nt; it >= 2; --it) {
-      k_bwd_uw_v<R><<<grid, 256, 0, st>>>(g, (const R*)e->pb, (R*)e->ub, (R*)e->wb, (const R*)e->pe, (R*)e->ue,
+      k_bwd_uw_v<R><<<grid, vec_block(e), 0, st>>>(g, (const R*)e->pb, (R*)e->ub, (R*)e->wb, (const R*)e->pe, (R*)e->ue,
                                           (R*)e->we, (const R*)e->strips, it, shot0);
-      k_bwd_p_v<R><<<grid, 256, 0, st>>>(g, make_rec(e), make_src(e), (const R*)e->src, (const R*)e->adj_t,
+      k_bwd_p_v<R><<<grid, vec_block(e), 0, st>>>(g, make_rec(e), make_src(e), (const R*)e->src, (const R*)e->adj_t,
                                          (R*)e->pb, (const R*)e->ub, (const R*)e->wb, (R*)e->pe, (const R*)e->ue,
                                          (const R*)e->we, (R*)e->dg, (R*)e->dfw, (R*)e->dbk, (const R*)e->strips, it,
                                          shot0);
@@ -625,11 +630,11 @@ int profile_impl(swit_engine* e, int32_t launches[4], double mean_ms[4], cudaStr
       if (e->variant == 3) {
         const dim3 vg = vec_grid(e, nb);
         record(0);
-        k_fwd_p_v<R><<<vg, 256, 0, st>>>(g, make_src(e), (const R*)e->src, (R*)e->p, (const R*)e->u, (const R*)e->w,
+        k_fwd_p_v<R><<<vg, vec_block(e), 0, st>>>(g, make_src(e), (const R*)e->src, (R*)e->p, (const R*)e->u, (const R*)e->w,
                                          it, s0);
         record(0);
         record(1);
-        k_fwd_uw_v<R><<<vg, 256, 0, st>>>(g, make_rec(e), (const R*)e->p, (R*)e->u, (R*)e->w, (R*)e->seis_t,
+        k_fwd_uw_v<R><<<vg, vec_block(e), 0, st>>>(g, make_rec(e), (const R*)e->p, (R*)e->u, (R*)e->w, (R*)e->seis_t,
                                           (R*)e->strips, it, s0);
         record(1);
         continue;
@@ -665,11 +670,11 @@ int profile_impl(swit_engine* e, int32_t launches[4], double mean_ms[4], cudaStr
       if (e->variant == 3) {
         const dim3 vg = vec_grid(e, nb);
         record(2);
-        k_bwd_uw_v<R><<<vg, 256, 0, st>>>(g, (const R*)e->pb, (R*)e->ub, (R*)e->wb, (const R*)e->pe, (R*)e->ue,
+        k_bwd_uw_v<R><<<vg, vec_block(e), 0, st>>>(g, (const R*)e->pb, (R*)e->ub, (R*)e->wb, (const R*)e->pe, (R*)e->ue,
                                           (R*)e->we, (const R*)e->strips, it, s0);
         record(2);
         record(3);
-        k_bwd_p_v<R><<<vg, 256, 0, st>>>(g, make_rec(e), make_src(e), (const R*)e->src, (const R*)e->adj_t,
+        k_bwd_p_v<R><<<vg, vec_block(e), 0, st>>>(g, make_rec(e), make_src(e), (const R*)e->src, (const R*)e->adj_t,
                                          (R*)e->pb, (const R*)e->ub, (const R*)e->wb, (R*)e->pe, (const R*)e->ue,
                                          (const R*)e->we, (R*)e->dg, (R*)e->dfw, (R*)e->dbk, (const R*)e->strips,
                                          it, s0);
@@ -763,7 +768,12 @@ int swit_create(const swit_desc* d, swit_engine** out) {
       return fail(SWIT_E_ARG, "block_x of the fused kernels must be 8, 16 or 32");
     }
   } else if (e->variant == 3) {
-    e->bx = 0;  // one thread per 4-row vector, 256 threads per block
+    // one thread per 4-row vector; blocks of 256 / block_x vectors x block_x columns
+    e->bx = d->block_x > 0 ? d->block_x : 32;
+    if (e->bx != 4 && e->bx != 8 && e->bx != 16 && e->bx != 32 && e->bx != 64) {
+      delete e;
+      return fail(SWIT_E_ARG, "block_x of the vec kernels must be 4, 8, 16, 32 or 64");
+    }
   } else {
     e->bx = d->block_x > 0 ? d->block_x : 4;
     if (32 * e->bx > 256 || (e->bx & (e->bx - 1))) {
@@ -834,6 +844,13 @@ int swit_create(const swit_desc* d, swit_engine** out) {
       cp[ix] = acc;
       acc += cnt[ix];
     }
+    int lo = 1 << 30, hi = -1;
+    for (size_t q = (size_t)base; q < e->ent_zr.size(); ++q) {
+      lo = std::min(lo, e->ent_zr[q]);
+      hi = std::max(hi, e->ent_zr[q]);
+    }
+    e->zlo.push_back(lo);
+    e->zhi.push_back(hi);
   }
   const size_t nent = std::max<size_t>(e->ent_ig.size(), 1);
   const size_t FSZ = (size_t)e->NX * e->LD, FSI = (size_t)e->nx * e->LDI;
@@ -850,6 +867,8 @@ int swit_create(const swit_desc* d, swit_engine** out) {
   AL(dalloc(e, &e->d_risx, ns));
   AL(dalloc(e, &e->d_risz, ns));
   AL(dalloc(e, &e->d_colptr, (size_t)ns * (NX + 2)));
+  AL(dalloc(e, &e->d_zlo, ns));
+  AL(dalloc(e, &e->d_zhi, ns));
   AL(dalloc(e, &e->d_ig, nent));
   AL(dalloc(e, &e->d_zr, nent));
   AL(dalloc(e, &e->d_live, (size_t)ns * ngm));
@@ -884,6 +903,7 @@ int swit_create(const swit_desc* d, swit_engine** out) {
       (rc = h2d(e->d_risx, e->risx.data(), ns * sizeof(int))) ||
       (rc = h2d(e->d_risz, e->risz.data(), ns * sizeof(int))) ||
       (rc = h2d(e->d_colptr, e->colptr.data(), e->colptr.size() * sizeof(int))) ||
+      (rc = h2d(e->d_zlo, e->zlo.data(), ns * sizeof(int))) || (rc = h2d(e->d_zhi, e->zhi.data(), ns * sizeof(int))) ||
       (e->ent_ig.size() && ((rc = h2d(e->d_ig, e->ent_ig.data(), e->ent_ig.size() * sizeof(int))) ||
                             (rc = h2d(e->d_zr, e->ent_zr.data(), e->ent_zr.size() * sizeof(int)))))) {
     release(e);

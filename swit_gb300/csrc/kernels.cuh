@@ -43,6 +43,8 @@ struct Receivers {
   const int* __restrict__ colptr;
   const int* __restrict__ ig;
   const int* __restrict__ zrow;
+  const int* __restrict__ zlo;  // per shot: lowest and highest receiver row (vectorised kernels;
+  const int* __restrict__ zhi;  // may be null elsewhere)
 };
 
 struct Sources {

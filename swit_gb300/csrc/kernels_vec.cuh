@@ -62,37 +62,36 @@ __device__ __forceinline__ void st4_except(R* p, size_t k4, const V4<R>& v, int 
     if (j != skip) p[4 * k4 + j] = v.x[j];
 }
 
-// Damping at (iz, ix), zero without any test in the interior block.
-template <class R>
-__device__ __forceinline__ R dampv(const Grid<R>& g, int iz, int ix) {
-  if (ix > g.L && ix <= g.NX - g.L && iz > g.L && iz <= g.NZ - g.L) return R(0);
-  return damp_at(g.damp, iz, ix, g.L, g.NX, g.NZ);
-}
+// Damping at (iz, ix) of a vector; one uniform test skips it for interior vectors.
+#define DAMPV(iz, ix) (v.dint ? R(0) : damp_at(g.damp, (iz), (ix), g.L, g.NX, g.NZ))
 
-// Thread -> (shot, column, first row) of its vector.
+// Thread -> (shot, column, first row) of its vector.  A block is a tile of
+// blockDim.x vectors along z by blockDim.y columns, so the x-neighbours a thread
+// reads are mostly the block's own columns (L1 hits).
 struct VecIdx {
   int s, ix, iz0, q;
   size_t k4;  // vector index within the shot
   bool ok;
+  bool dint;  // columns ix, ix+1 and rows iz0..iz0+4 all interior: every damping term is 0
 };
 template <class R>
 __device__ __forceinline__ VecIdx vec_index(const Grid<R>& g, int shot0) {
   VecIdx v;
   const int LD4 = g.LD >> 2;
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  v.s = shot0 + blockIdx.y;
-  v.ok = t < g.NX * LD4;
-  v.ix = t / LD4 + 1;
-  v.q = t - (v.ix - 1) * LD4;
+  v.s = shot0 + blockIdx.z;
+  v.q = blockIdx.x * blockDim.x + threadIdx.x;
+  v.ix = blockIdx.y * blockDim.y + threadIdx.y + 1;
+  v.ok = v.q < LD4 && v.ix <= g.NX;
   v.iz0 = 4 * v.q + 1;
-  v.k4 = (size_t)t;
+  v.k4 = (size_t)(v.ix - 1) * LD4 + v.q;
+  v.dint = v.ix > g.L && v.ix + 1 <= g.NX - g.L && v.iz0 > g.L && v.iz0 + 4 <= g.NZ - g.L;
   return v;
 }
 
 // ---------------------------------------------------------------------------
 // Forward pressure phase (fdcore.f90:77-94).
 template <class R>
-__global__ void __launch_bounds__(256) k_fwd_p_v(Grid<R> g, Sources src, const R* __restrict__ s_fwd, R* P,
+__global__ void __launch_bounds__(256, 5) k_fwd_p_v(Grid<R> g, Sources src, const R* __restrict__ s_fwd, R* P,
                                                  const R* __restrict__ U, const R* __restrict__ W, int it, int shot0) {
   const VecIdx v = vec_index(g, shot0);
   if (!v.ok) return;
@@ -124,7 +123,7 @@ __global__ void __launch_bounds__(256) k_fwd_p_v(Grid<R> g, Sources src, const R
     for (int j = 0; j < 4; ++j) {
       const int iz = iz0 + j;
       if (iz >= fs + 1 && iz <= NZ - 2) {
-        const R kappa = dampv(g, iz, ix) * g.dt;
+        const R kappa = DAMPV(iz, ix) * g.dt;
         pv.x[j] = (R(1.0) - kappa) * pv.x[j] -
                   a.x[j] * (g.c1 * (u0.x[j] - um1.x[j] + wz[j + 2] - wz[j + 1]) +
                             g.c2 * (up1.x[j] - um2.x[j] + wz[j + 3] - wz[j]));
@@ -175,7 +174,7 @@ __global__ void __launch_bounds__(256) k_fwd_uw_v(Grid<R> g, Receivers rec, cons
       for (int j = 0; j < 4; ++j) {
         const int iz = iz0 + j;
         if (iz >= fs && iz <= NZ - 1) {
-          const R kappa = R(0.5) * (dampv(g, iz, ix) + dampv(g, iz, ix + 1)) * g.dt;
+          const R kappa = R(0.5) * (DAMPV(iz, ix) + DAMPV(iz, ix + 1)) * g.dt;
           uv.x[j] = (R(1.0) - kappa) * uv.x[j] - b.x[j] * (g.c1 * (pp1.x[j] - p0.x[j]) + g.c2 * (pp2.x[j] - pm1.x[j]));
         }
       }
@@ -198,7 +197,7 @@ __global__ void __launch_bounds__(256) k_fwd_uw_v(Grid<R> g, Receivers rec, cons
     for (int j = 0; j < 4; ++j) {
       const int iz = iz0 + j;
       if (iz >= fs && iz <= NZ - 2) {
-        const R kappa = R(0.5) * (dampv(g, iz, ix) + dampv(g, iz + 1, ix)) * g.dt;
+        const R kappa = R(0.5) * (DAMPV(iz, ix) + DAMPV(iz + 1, ix)) * g.dt;
         wv.x[j] = (R(1.0) - kappa) * wv.x[j] - b.x[j] * (g.c1 * (pz[j + 2] - pz[j + 1]) + g.c2 * (pz[j + 3] - pz[j]));
       }
     }
@@ -219,7 +218,7 @@ __global__ void __launch_bounds__(256) k_fwd_uw_v(Grid<R> g, Receivers rec, cons
   if (du) st4(u, v.k4, uv);
   if (dw) st4(w, v.k4, wv);
   // receivers (fdcore.f90:123-128)
-  {
+  if (iz0 + 3 >= rec.zlo[v.s] && iz0 <= rec.zhi[v.s]) {
     const int* cp = rec.colptr + (size_t)v.s * (NX + 2);
     const int e1 = cp[ix + 1];
     for (int e = cp[ix]; e < e1; ++e) {
@@ -227,7 +226,9 @@ __global__ void __launch_bounds__(256) k_fwd_uw_v(Grid<R> g, Receivers rec, cons
       if (j >= 0 && j < 4) seis_t[((size_t)v.s * g.nt + (it - 1)) * g.ngmax + rec.ig[e]] = p0.x[j];
     }
   }
-  if (strips) {
+  const bool strip_rows = (iz0 <= fs + 2 && iz0 + 3 >= fs) || (iz0 <= NZ - L && iz0 + 3 >= NZ - L - 1);
+  const bool strip_cols = ix == L + 1 || ix == L + 2 || ix == NX - L || ix == NX - L - 1;
+  if (strips && (strip_rows || strip_cols)) {
     R* b = strips + ((size_t)v.s * g.nt + (it - 1)) * g.SL;
     const StripOff o = strip_offsets(g.nx, g.nz);
     const int jx = ix - L;
@@ -292,7 +293,7 @@ __global__ void __launch_bounds__(256) k_bwd_uw_v(Grid<R> g, const R* __restrict
       for (int j = 0; j < 4; ++j) {
         const int iz = iz0 + j;
         if (iz >= 2 && iz <= NZ - 1) {
-          const R kappa = R(0.5) * (dampv(g, iz, ix) + dampv(g, iz, ix + 1)) * g.dt;
+          const R kappa = R(0.5) * (DAMPV(iz, ix) + DAMPV(iz, ix + 1)) * g.dt;
           uv.x[j] = (R(1.0) - kappa) * uv.x[j] - a.x[j] * (g.c1 * (pp1.x[j] - p0.x[j]) + g.c2 * (pp2.x[j] - pm1.x[j]));
         }
       }
@@ -316,7 +317,7 @@ __global__ void __launch_bounds__(256) k_bwd_uw_v(Grid<R> g, const R* __restrict
     for (int j = 0; j < 4; ++j) {
       const int iz = iz0 + j;
       if (iz >= 2 && iz <= NZ - 2) {
-        const R kappa = R(0.5) * (dampv(g, iz, ix) + dampv(g, iz + 1, ix)) * g.dt;
+        const R kappa = R(0.5) * (DAMPV(iz, ix) + DAMPV(iz + 1, ix)) * g.dt;
         wv.x[j] = (R(1.0) - kappa) * wv.x[j] - a.x[j] * (g.c1 * (pz[j + 2] - pz[j + 1]) + g.c2 * (pz[j + 3] - pz[j]));
       }
     }
@@ -430,7 +431,7 @@ __global__ void __launch_bounds__(256) k_bwd_p_v(Grid<R> g, Receivers rec, Sourc
     for (int j = 0; j < 4; ++j) {
       const int iz = iz0 + j;
       if (iz >= 3 && iz <= NZ - 2) {
-        const R kappa = dampv(g, iz, ix) * g.dt;
+        const R kappa = DAMPV(iz, ix) * g.dt;
         pv.x[j] = (R(1.0) - kappa) * pv.x[j] -
                   bcoef.x[j] * (g.c1 * (u0.x[j] - um1.x[j] + wz[j + 2] - wz[j + 1]) +
                                 g.c2 * (up1.x[j] - um2.x[j] + wz[j + 3] - wz[j]));
@@ -438,7 +439,7 @@ __global__ void __launch_bounds__(256) k_bwd_p_v(Grid<R> g, Receivers rec, Sourc
     }
     dirty = true;
   }
-  {
+  if (iz0 + 3 >= rec.zlo[v.s] && iz0 <= rec.zhi[v.s]) {
     const int* cp = rec.colptr + (size_t)v.s * (NX + 2);
     const int e1 = cp[ix + 1];
     for (int e = cp[ix]; e < e1; ++e) {

@@ -98,7 +98,8 @@ def test_gradient_l2_single_call_matches_oracle(base):
                                   dict(kernel="split"), dict(kernel="split", block_x=8),
                                   dict(kernel="split", block_x=1), dict(kernel="split", path="plain"),
                                   dict(kernel="split", shots_per_batch=2), dict(kernel="vec"),
-                                  dict(kernel="vec", path="plain"), dict(kernel="vec", shots_per_batch=2)])
+                                  dict(kernel="vec", path="plain"), dict(kernel="vec", shots_per_batch=2),
+                                  dict(kernel="vec", block_x=4), dict(kernel="vec", block_x=64)])
 def test_launch_variants_are_identical(base, opts):
     s = base["s"]
     with engine(s, **opts) as e:
