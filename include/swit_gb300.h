@@ -128,6 +128,16 @@ int swit_gradient_l2(swit_engine* e, const float* src, const float* obs, void* g
 int swit_export_snapshot(swit_engine* e, void* boundary, void* p_end, void* u_end, void* w_end, int on_device,
                          void* stream);
 
+/* Loads a saved forward run instead of computing one: the forward source
+ * (ns, nt), the boundary strips in boundary.bin layout (ns, nt, 9 nx + 6 nz) and
+ * the final interior wavefields p_end, u_end, w_end (ns, nx, nz) -- the inputs
+ * fd2dmpi's adjoint job reads from parfile/forward_source and
+ * <DATA_OUT>N_snapshot/ (fd2dmpi/solver.f90:212-228).  A following
+ * swit_backward then needs no swit_forward.  Inputs are float in both
+ * precisions (the reference's file format). */
+int swit_import_snapshot(swit_engine* e, const float* src, const float* boundary, const float* p_end,
+                         const float* u_end, const float* w_end, int on_device, void* stream);
+
 /* Profiling hook (the reference has none; fd2dmpi only prints banners,
  * fd2dmpi/solver.f90:78-84).  Re-runs the forward loop (with strips) and the
  * reverse loop on the inputs staged by the last swit_gradient_l2 or

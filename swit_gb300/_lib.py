@@ -15,7 +15,7 @@ ERRORS = {-1: "SWIT_E_ARG", -2: "SWIT_E_GEOM", -3: "SWIT_E_CFL", -4: "SWIT_E_MOD
 
 # every symbol include/swit_gb300.h declares
 EXPORTS = ("swit_create", "swit_set_model", "swit_forward", "swit_backward", "swit_gradient_l2",
-           "swit_export_snapshot", "swit_profile_kernels", "swit_query", "swit_destroy", "swit_last_error", "swit_damp_profile",
+           "swit_export_snapshot", "swit_import_snapshot", "swit_profile_kernels", "swit_query", "swit_destroy", "swit_last_error", "swit_damp_profile",
            "swit_forward_shot_static")
 
 
@@ -57,6 +57,7 @@ def load(build_if_missing: bool = True):
         "swit_backward": ([vp, vp, vp, vp, vp, i, vp], i),
         "swit_gradient_l2": ([vp, vp, vp, vp, vp, vp, vp, C.POINTER(C.c_double), i, vp], i),
         "swit_export_snapshot": ([vp, vp, vp, vp, vp, i, vp], i),
+        "swit_import_snapshot": ([vp, vp, vp, vp, vp, vp, i, vp], i),
         "swit_profile_kernels": ([vp, C.POINTER(C.c_int32), C.POINTER(C.c_double), vp], i),
         "swit_query": ([vp, C.POINTER(C.c_int64), C.POINTER(C.c_int32), C.POINTER(C.c_int32),
                         C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.POINTER(C.c_int32)], i),

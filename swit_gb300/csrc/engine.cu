@@ -710,6 +710,41 @@ int profile_impl(swit_engine* e, int32_t launches[4], double mean_ms[4], cudaStr
   return 0;
 }
 
+// Saved forward run -> source, strips and final forward state (the buffers copy_end reads).
+template <class R>
+int import_impl(swit_engine* e, const float* src, const float* boundary, const float* pend, const float* uend,
+                const float* wend, int on_device, cudaStream_t st) {
+  Grid<R> g = make_grid<R>(e);
+  const size_t NB = (size_t)e->ns * e->nt * e->SL, NI = (size_t)e->ns * e->nx * e->nz;
+  const bool in_b = e->variant == 2 && (e->nt - 2) % 2 == 0;
+  void* finals[3] = {in_b ? e->p2 : e->p, in_b ? e->u2 : e->u, in_b ? e->w2 : e->w};
+  const float* ends[3] = {pend, uend, wend};
+  auto staged = [&](const float* in, size_t n, float** tmp) -> int {
+    *tmp = nullptr;
+    if (on_device) return 0;
+    CK(cudaMallocAsync((void**)tmp, n * sizeof(float), st));
+    CK(cudaMemcpyAsync(*tmp, in, n * sizeof(float), cudaMemcpyHostToDevice, st));
+    return 0;
+  };
+  float* tmp = nullptr;
+  int rc = staged(src, (size_t)e->ns * e->nt, &tmp);
+  if (rc) return rc;
+  k_src_in<R><<<nblocks((size_t)e->ns * (e->nt + 1)), 256, 0, st>>>(tmp ? tmp : src, (R*)e->src, e->ns, e->nt);
+  if (tmp) CK(cudaFreeAsync(tmp, st));
+  if ((rc = staged(boundary, NB, &tmp))) return rc;
+  k_strips_in<R><<<nblocks(NB), 256, 0, st>>>(g, tmp ? tmp : boundary, (R*)e->strips, e->ns);
+  if (tmp) CK(cudaFreeAsync(tmp, st));
+  for (int q = 0; q < 3; ++q) {
+    if ((rc = staged(ends[q], NI, &tmp))) return rc;
+    k_end_in<R><<<nblocks(NI), 256, 0, st>>>(g, tmp ? tmp : ends[q], (R*)finals[q], e->ns);
+    if (tmp) CK(cudaFreeAsync(tmp, st));
+  }
+  CK(cudaGetLastError());
+  if (!on_device) CK(cudaStreamSynchronize(st));
+  e->fwd_ready = true;
+  return 0;
+}
+
 // Grid index npml + int(x/dx) + 1 in single precision (fdcore.f90:70, 124).
 inline int gidx(int L, float x, float dx) { return L + (int)(x / dx) + 1; }
 
@@ -991,6 +1026,15 @@ int swit_export_snapshot(swit_engine* e, void* boundary, void* p_end, void* u_en
   cudaStream_t st = (cudaStream_t)stream;
   return e->prec ? export_impl<double>(e, boundary, p_end, u_end, w_end, on_device, st)
                  : export_impl<float>(e, boundary, p_end, u_end, w_end, on_device, st);
+}
+
+int swit_import_snapshot(swit_engine* e, const float* src, const float* boundary, const float* p_end,
+                         const float* u_end, const float* w_end, int on_device, void* stream) {
+  if (!e || !src || !boundary || !p_end || !u_end || !w_end) return fail(SWIT_E_ARG, "null argument");
+  if (!e->model_set) return fail(SWIT_E_STATE, "swit_set_model must be called before swit_import_snapshot");
+  cudaStream_t st = (cudaStream_t)stream;
+  return e->prec ? import_impl<double>(e, src, boundary, p_end, u_end, w_end, on_device, st)
+                 : import_impl<float>(e, src, boundary, p_end, u_end, w_end, on_device, st);
 }
 
 int swit_profile_kernels(swit_engine* e, int32_t launches[4], double mean_ms[4], void* stream) {

@@ -520,4 +520,42 @@ __global__ void k_strips_out(Grid<R> g, const R* __restrict__ strips, O* out, in
   }
 }
 
+// The reference's interleaved boundary(S, nt) layout (float) -> strips (SoA per step).
+template <class R>
+__global__ void k_strips_in(Grid<R> g, const float* __restrict__ in, R* strips, int ns) {
+  const int nx = g.nx, nz = g.nz, SL = g.SL;
+  const size_t n = (size_t)ns * g.nt * SL;
+  const StripOff o = strip_offsets(nx, nz);
+  for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x) {
+    const size_t rec = t / SL;
+    const int q = (int)(t - rec * SL);
+    R* b = strips + rec * SL;
+    const R v = (R)in[t];
+    if (q < 3 * nx) {
+      const int j = q / 3, e = q - 3 * j;
+      b[(e == 0 ? o.B0 : e == 1 ? o.B1 : o.B2) + j] = v;
+    } else if (q < 3 * nx + 6 * nz) {
+      const int r = (q - 3 * nx) / 6, e = (q - 3 * nx) - 6 * r;
+      const int seg[6] = {o.S0, o.S1, o.S2, o.S3, o.S4, o.S5};
+      b[seg[e] + r] = v;
+    } else {
+      const int j = (q - 3 * nx - 6 * nz) / 6, e = (q - 3 * nx - 6 * nz) - 6 * j;
+      const int seg[6] = {o.T0, o.T1, o.T2, o.T3, o.T4, o.T5};
+      b[seg[e] + j] = v;
+    }
+  }
+}
+
+// (ns, nx, nz) float -> interior points of a PML-grid field (the final forward state).
+template <class R>
+__global__ void k_end_in(Grid<R> g, const float* __restrict__ in, R* F, int ns) {
+  const size_t n = (size_t)ns * g.nx * g.nz;
+  for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x) {
+    const int s = (int)(t / ((size_t)g.nx * g.nz));
+    const int r = (int)(t - (size_t)s * g.nx * g.nz);
+    const int jx = r / g.nz, jz = r - jx * g.nz;
+    F[(size_t)s * g.FSZ + (size_t)(jx + g.L) * g.LD + (jz + g.L)] = (R)in[t];
+  }
+}
+
 }  // namespace swit

@@ -62,9 +62,6 @@ __device__ __forceinline__ void st4_except(R* p, size_t k4, const V4<R>& v, int 
     if (j != skip) p[4 * k4 + j] = v.x[j];
 }
 
-// Damping at (iz, ix) of a vector; one uniform test skips it for interior vectors.
-#define DAMPV(iz, ix) (v.dint ? R(0) : damp_at(g.damp, (iz), (ix), g.L, g.NX, g.NZ))
-
 // Thread -> (shot, column, first row) of its vector.  A block is a tile of
 // blockDim.x vectors along z by blockDim.y columns, so the x-neighbours a thread
 // reads are mostly the block's own columns (L1 hits).
@@ -73,6 +70,8 @@ struct VecIdx {
   size_t k4;  // vector index within the shot
   bool ok;
   bool dint;  // columns ix, ix+1 and rows iz0..iz0+4 all interior: every damping term is 0
+  bool deep;  // columns [L+3, NX-L-3], rows [L+4, NZ-L-3]: every update range holds, no
+              // strip, mirror or re-insert row or column, no damping
 };
 template <class R>
 __device__ __forceinline__ VecIdx vec_index(const Grid<R>& g, int shot0) {
@@ -85,44 +84,64 @@ __device__ __forceinline__ VecIdx vec_index(const Grid<R>& g, int shot0) {
   v.iz0 = 4 * v.q + 1;
   v.k4 = (size_t)(v.ix - 1) * LD4 + v.q;
   v.dint = v.ix > g.L && v.ix + 1 <= g.NX - g.L && v.iz0 > g.L && v.iz0 + 4 <= g.NZ - g.L;
+  v.deep = v.ix >= g.L + 3 && v.ix <= g.NX - g.L - 3 && v.iz0 >= g.L + 4 && v.iz0 + 3 <= g.NZ - g.L - 3;
   return v;
+}
+
+// Damping at (iz, ix) of a vector: 0 on the fast path and for interior vectors.
+#define DAMPV(iz, ix) ((FAST || v.dint) ? R(0) : damp_at(g.damp, (iz), (ix), g.L, g.NX, g.NZ))
+
+// z-neighbours: the rows iz0+lo .. iz0+4+hi-1 of column ix around vector k4, as an
+// array r[0 .. 4-lo+hi-1] (r[-lo] is row iz0); rows outside the column read 0.
+template <class R>
+__device__ __forceinline__ void col_window(const R* f, const VecIdx& v, int LD4, const V4<R>& own, R* r, int lo,
+                                           int hi) {
+  // lo in {-2, -1}, hi in {1, 2}
+  if (v.q > 0) {
+    const V4<R> m = ld4(f, v.k4 - 1);
+    if (lo == -2) {
+      r[0] = m.x[2];
+      r[1] = m.x[3];
+    } else {
+      r[0] = m.x[3];
+    }
+  } else {
+    r[0] = R(0);
+    if (lo == -2) r[1] = R(0);
+  }
+  const int o = -lo;
+  r[o] = own.x[0];
+  r[o + 1] = own.x[1];
+  r[o + 2] = own.x[2];
+  r[o + 3] = own.x[3];
+  if (v.q + 1 < LD4) {
+    const V4<R> n = ld4(f, v.k4 + 1);
+    r[o + 4] = n.x[0];
+    if (hi == 2) r[o + 5] = n.x[1];
+  } else {
+    r[o + 4] = R(0);
+    if (hi == 2) r[o + 5] = R(0);
+  }
 }
 
 // ---------------------------------------------------------------------------
 // Forward pressure phase (fdcore.f90:77-94).
-template <class R>
-__global__ void __launch_bounds__(256, 5) k_fwd_p_v(Grid<R> g, Sources src, const R* __restrict__ s_fwd, R* P,
-                                                 const R* __restrict__ U, const R* __restrict__ W, int it, int shot0) {
-  const VecIdx v = vec_index(g, shot0);
-  if (!v.ok) return;
+template <class R, bool FAST>
+__device__ __forceinline__ void fwd_p_body(const Grid<R>& g, const Sources& src, const R* __restrict__ s_fwd, R* __restrict__ p,
+                                           const R* __restrict__ u, const R* __restrict__ w, int it,
+                                           const VecIdx& v) {
   const int LD4 = g.LD >> 2, ix = v.ix, iz0 = v.iz0, fs = g.fs, NZ = g.NZ;
-  const size_t off = (size_t)v.s * g.FSZ;
-  R* p = P + off;
-  const R* u = U + off;
-  const R* w = W + off;
   V4<R> pv = ld4(p, v.k4);
   bool dirty = false;
-  if (ix >= 3 && ix <= g.NX - 2 && iz0 + 3 >= fs + 1 && iz0 <= NZ - 2) {
+  if (FAST || (ix >= 3 && ix <= g.NX - 2 && iz0 + 3 >= fs + 1 && iz0 <= NZ - 2)) {
     const V4<R> a = ld4(g.A, v.k4);
     const V4<R> u0 = ld4(u, v.k4), um1 = ld4(u, v.k4 - LD4), up1 = ld4(u, v.k4 + LD4), um2 = ld4(u, v.k4 - 2 * LD4);
     R wz[7];  // w at rows iz0-2 .. iz0+4
-    const V4<R> w0 = ld4(w, v.k4);
-    wz[2] = w0.x[0];
-    wz[3] = w0.x[1];
-    wz[4] = w0.x[2];
-    wz[5] = w0.x[3];
-    if (v.q > 0) {
-      const V4<R> wm = ld4(w, v.k4 - 1);
-      wz[0] = wm.x[2];
-      wz[1] = wm.x[3];
-    } else {
-      wz[0] = wz[1] = R(0);
-    }
-    wz[6] = (v.q + 1 < LD4) ? w[(size_t)ix * g.LD - g.LD + iz0 + 3] : R(0);
+    col_window(w, v, LD4, ld4(w, v.k4), wz, -2, 1);
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
       const int iz = iz0 + j;
-      if (iz >= fs + 1 && iz <= NZ - 2) {
+      if (FAST || (iz >= fs + 1 && iz <= NZ - 2)) {
         const R kappa = DAMPV(iz, ix) * g.dt;
         pv.x[j] = (R(1.0) - kappa) * pv.x[j] -
                   a.x[j] * (g.c1 * (u0.x[j] - um1.x[j] + wz[j + 2] - wz[j + 1]) +
@@ -131,49 +150,58 @@ __global__ void __launch_bounds__(256, 5) k_fwd_p_v(Grid<R> g, Sources src, cons
     }
     dirty = true;
   }
-  const int js = src.isz[v.s] - iz0;
-  if (ix == src.isx[v.s] && js >= 0 && js < 4) {
-    pv.x[js] = pv.x[js] + g.dt * s_fwd[(size_t)v.s * (g.nt + 1) + (it - 1)];
-    dirty = true;
-  }
-  // p(fs-1, :) = -p(fs+1, :) (fdcore.f90:92-94).  Rows fs-1 and fs+1 share a
-  // vector, or row fs-1 is in the vector above, whose rows (<= fs) this phase
-  // never changes: its owner stores nothing and the owner of fs+1 writes it.
-  const int jm = fs - 1 - iz0, jp = fs + 1 - iz0;
-  if (g.fs_flag == 1 && jp >= 0 && jp < 4) {
-    if (jm >= 0) {
-      pv.x[jm] = -pv.x[jp];
+  if (!FAST) {
+    const int js = src.isz[v.s] - iz0;
+    if (ix == src.isx[v.s] && js >= 0 && js < 4) {
+      pv.x[js] = pv.x[js] + g.dt * s_fwd[(size_t)v.s * (g.nt + 1) + (it - 1)];
       dirty = true;
-    } else {
-      p[(size_t)(ix - 1) * g.LD + (fs - 2)] = -pv.x[jp];
+    }
+    // p(fs-1, :) = -p(fs+1, :) (fdcore.f90:92-94).  Rows fs-1 and fs+1 share a
+    // vector, or row fs-1 is in the vector above, whose rows (<= fs) this phase
+    // never changes: its owner stores nothing and the owner of fs+1 writes it.
+    const int jm = fs - 1 - iz0, jp = fs + 1 - iz0;
+    if (g.fs_flag == 1 && jp >= 0 && jp < 4) {
+      if (jm >= 0) {
+        pv.x[jm] = -pv.x[jp];
+        dirty = true;
+      } else {
+        p[(size_t)(ix - 1) * g.LD + (fs - 2)] = -pv.x[jp];
+      }
     }
   }
   if (dirty) st4(p, v.k4, pv);
 }
 
-// Forward velocity phase (fdcore.f90:97-159).
 template <class R>
-__global__ void __launch_bounds__(256) k_fwd_uw_v(Grid<R> g, Receivers rec, const R* __restrict__ P, R* U, R* W,
-                                                  R* __restrict__ seis_t, R* __restrict__ strips, int it, int shot0) {
+__global__ void __launch_bounds__(256) k_fwd_p_v(Grid<R> g, Sources src, const R* __restrict__ s_fwd, R* P,
+                                                 const R* __restrict__ U, const R* __restrict__ W, int it, int shot0) {
   const VecIdx v = vec_index(g, shot0);
   if (!v.ok) return;
-  const int LD4 = g.LD >> 2, ix = v.ix, iz0 = v.iz0, fs = g.fs, NZ = g.NZ, NX = g.NX, L = g.L;
   const size_t off = (size_t)v.s * g.FSZ;
-  const R* p = P + off;
-  R* u = U + off;
-  R* w = W + off;
+  const bool src_here = v.ix == src.isx[v.s] && src.isz[v.s] >= v.iz0 && src.isz[v.s] < v.iz0 + 4;
+  if (v.deep && !src_here)
+    fwd_p_body<R, true>(g, src, s_fwd, P + off, U + off, W + off, it, v);
+  else
+    fwd_p_body<R, false>(g, src, s_fwd, P + off, U + off, W + off, it, v);
+}
+
+// Forward velocity phase (fdcore.f90:97-159).
+template <class R, bool FAST>
+__device__ __forceinline__ void fwd_uw_body(const Grid<R>& g, const Receivers& rec, const R* __restrict__ p, R* __restrict__ u,
+                                            R* __restrict__ w, R* __restrict__ seis_t, R* __restrict__ strips, int it,
+                                            const VecIdx& v) {
+  const int LD4 = g.LD >> 2, ix = v.ix, iz0 = v.iz0, fs = g.fs, NZ = g.NZ, NX = g.NX, L = g.L;
   const V4<R> p0 = ld4(p, v.k4);
   V4<R> uv = ld4(u, v.k4), wv = ld4(w, v.k4);
   bool du = false, dw = false;
-  const bool rows = iz0 + 3 >= fs && iz0 <= NZ - 1;
-  if (rows && ix >= 2 && ix <= NX - 1) {
+  if (FAST || (iz0 + 3 >= fs && iz0 <= NZ - 1 && ix >= 2 && ix <= NX - 1)) {
     const V4<R> b = ld4(g.B, v.k4);
-    if (ix <= NX - 2) {
+    if (FAST || ix <= NX - 2) {
       const V4<R> pp1 = ld4(p, v.k4 + LD4), pp2 = ld4(p, v.k4 + 2 * LD4), pm1 = ld4(p, v.k4 - LD4);
 #pragma unroll
       for (int j = 0; j < 4; ++j) {
         const int iz = iz0 + j;
-        if (iz >= fs && iz <= NZ - 1) {
+        if (FAST || (iz >= fs && iz <= NZ - 1)) {
           const R kappa = R(0.5) * (DAMPV(iz, ix) + DAMPV(iz, ix + 1)) * g.dt;
           uv.x[j] = (R(1.0) - kappa) * uv.x[j] - b.x[j] * (g.c1 * (pp1.x[j] - p0.x[j]) + g.c2 * (pp2.x[j] - pm1.x[j]));
         }
@@ -181,42 +209,34 @@ __global__ void __launch_bounds__(256) k_fwd_uw_v(Grid<R> g, Receivers rec, cons
       du = true;
     }
     R pz[7];  // p at rows iz0-1 .. iz0+5
-    pz[1] = p0.x[0];
-    pz[2] = p0.x[1];
-    pz[3] = p0.x[2];
-    pz[4] = p0.x[3];
-    pz[0] = v.q > 0 ? p[(size_t)(ix - 1) * g.LD + iz0 - 2] : R(0);
-    if (v.q + 1 < LD4) {
-      const V4<R> pn = ld4(p, v.k4 + 1);
-      pz[5] = pn.x[0];
-      pz[6] = pn.x[1];
-    } else {
-      pz[5] = pz[6] = R(0);
-    }
+    col_window(p, v, LD4, p0, pz, -1, 2);
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
       const int iz = iz0 + j;
-      if (iz >= fs && iz <= NZ - 2) {
+      if (FAST || (iz >= fs && iz <= NZ - 2)) {
         const R kappa = R(0.5) * (DAMPV(iz, ix) + DAMPV(iz + 1, ix)) * g.dt;
         wv.x[j] = (R(1.0) - kappa) * wv.x[j] - b.x[j] * (g.c1 * (pz[j + 2] - pz[j + 1]) + g.c2 * (pz[j + 3] - pz[j]));
       }
     }
     dw = true;
   }
-  // w(fs-1, ix) = w(fs, ix) for every column (fdcore.f90:116-120).  If row
-  // fs-1 ends the vector above, that vector (rows < fs) has no u or w update
-  // and its owner stores nothing; the owner of row fs writes the mirror.
-  const int jm = fs - 1 - iz0, jr = fs - iz0;
-  if (g.fs_flag == 1 && jr >= 0 && jr < 4) {
-    if (jm >= 0) {
-      wv.x[jm] = wv.x[jr];
-      dw = true;
-    } else {
-      w[(size_t)(ix - 1) * g.LD + (fs - 2)] = wv.x[jr];
+  if (!FAST) {
+    // w(fs-1, ix) = w(fs, ix) for every column (fdcore.f90:116-120).  If row
+    // fs-1 ends the vector above, that vector (rows < fs) has no u or w update
+    // and its owner stores nothing; the owner of row fs writes the mirror.
+    const int jm = fs - 1 - iz0, jr = fs - iz0;
+    if (g.fs_flag == 1 && jr >= 0 && jr < 4) {
+      if (jm >= 0) {
+        wv.x[jm] = wv.x[jr];
+        dw = true;
+      } else {
+        w[(size_t)(ix - 1) * g.LD + (fs - 2)] = wv.x[jr];
+      }
     }
   }
   if (du) st4(u, v.k4, uv);
   if (dw) st4(w, v.k4, wv);
+  if (FAST) return;
   // receivers (fdcore.f90:123-128)
   if (iz0 + 3 >= rec.zlo[v.s] && iz0 <= rec.zhi[v.s]) {
     const int* cp = rec.colptr + (size_t)v.s * (NX + 2);
@@ -226,73 +246,81 @@ __global__ void __launch_bounds__(256) k_fwd_uw_v(Grid<R> g, Receivers rec, cons
       if (j >= 0 && j < 4) seis_t[((size_t)v.s * g.nt + (it - 1)) * g.ngmax + rec.ig[e]] = p0.x[j];
     }
   }
+  // boundary strips of step it (fdcore.f90:130-159)
   const bool strip_rows = (iz0 <= fs + 2 && iz0 + 3 >= fs) || (iz0 <= NZ - L && iz0 + 3 >= NZ - L - 1);
   const bool strip_cols = ix == L + 1 || ix == L + 2 || ix == NX - L || ix == NX - L - 1;
   if (strips && (strip_rows || strip_cols)) {
-    R* b = strips + ((size_t)v.s * g.nt + (it - 1)) * g.SL;
+    R* bs = strips + ((size_t)v.s * g.nt + (it - 1)) * g.SL;
     const StripOff o = strip_offsets(g.nx, g.nz);
     const int jx = ix - L;
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
       const int iz = iz0 + j, jz = iz - L;
       if (jx >= 1 && jx <= g.nx) {
-        if (iz == NZ - L) b[o.B0 + jx - 1] = p0.x[j];
+        if (iz == NZ - L) bs[o.B0 + jx - 1] = p0.x[j];
         if (iz == NZ - L - 1) {
-          b[o.B1 + jx - 1] = p0.x[j];
-          b[o.B2 + jx - 1] = wv.x[j];
+          bs[o.B1 + jx - 1] = p0.x[j];
+          bs[o.B2 + jx - 1] = wv.x[j];
         }
         if (iz == fs) {
-          b[o.T0 + jx - 1] = p0.x[j];
-          b[o.T3 + jx - 1] = uv.x[j];
-          b[o.T5 + jx - 1] = wv.x[j];
+          bs[o.T0 + jx - 1] = p0.x[j];
+          bs[o.T3 + jx - 1] = uv.x[j];
+          bs[o.T5 + jx - 1] = wv.x[j];
         }
         if (iz == fs + 1) {
-          b[o.T1 + jx - 1] = p0.x[j];
-          b[o.T4 + jx - 1] = uv.x[j];
+          bs[o.T1 + jx - 1] = p0.x[j];
+          bs[o.T4 + jx - 1] = uv.x[j];
         }
-        if (iz == fs + 2) b[o.T2 + jx - 1] = p0.x[j];
+        if (iz == fs + 2) bs[o.T2 + jx - 1] = p0.x[j];
       }
       if (jz >= 1 && jz <= g.nz) {
         if (ix == L + 1) {
-          b[o.S0 + jz - 1] = p0.x[j];
-          b[o.S2 + jz - 1] = uv.x[j];
+          bs[o.S0 + jz - 1] = p0.x[j];
+          bs[o.S2 + jz - 1] = uv.x[j];
         }
-        if (ix == L + 2) b[o.S1 + jz - 1] = p0.x[j];
-        if (ix == NX - L) b[o.S3 + jz - 1] = p0.x[j];
+        if (ix == L + 2) bs[o.S1 + jz - 1] = p0.x[j];
+        if (ix == NX - L) bs[o.S3 + jz - 1] = p0.x[j];
         if (ix == NX - L - 1) {
-          b[o.S4 + jz - 1] = p0.x[j];
-          b[o.S5 + jz - 1] = uv.x[j];
+          bs[o.S4 + jz - 1] = p0.x[j];
+          bs[o.S5 + jz - 1] = uv.x[j];
         }
       }
     }
   }
 }
 
+template <class R>
+__global__ void __launch_bounds__(256) k_fwd_uw_v(Grid<R> g, Receivers rec, const R* __restrict__ P, R* U, R* W,
+                                                  R* __restrict__ seis_t, R* __restrict__ strips, int it, int shot0) {
+  const VecIdx v = vec_index(g, shot0);
+  if (!v.ok) return;
+  const size_t off = (size_t)v.s * g.FSZ;
+  const bool rec_here = v.iz0 + 3 >= rec.zlo[v.s] && v.iz0 <= rec.zhi[v.s];
+  if (v.deep && !rec_here)
+    fwd_uw_body<R, true>(g, rec, P + off, U + off, W + off, seis_t, strips, it, v);
+  else
+    fwd_uw_body<R, false>(g, rec, P + off, U + off, W + off, seis_t, strips, it, v);
+}
+
 // ---------------------------------------------------------------------------
 // Backward velocity phase: adjoint u, w (fdcore.f90:309-333) and the
 // reconstruction u, w with their re-insert (fdcore.f90:220-247).
-template <class R>
-__global__ void __launch_bounds__(256) k_bwd_uw_v(Grid<R> g, const R* __restrict__ PB, R* UB, R* WB,
-                                                  const R* __restrict__ PE, R* UE, R* WE,
-                                                  const R* __restrict__ strips, int it, int shot0) {
-  const VecIdx v = vec_index(g, shot0);
-  if (!v.ok) return;
+template <class R, bool FAST>
+__device__ __forceinline__ void bwd_uw_body(const Grid<R>& g, const R* __restrict__ pb, R* __restrict__ ub, R* __restrict__ wb,
+                                            const R* __restrict__ pe, R* __restrict__ ue, R* __restrict__ we, const R* __restrict__ strips,
+                                            int it, const VecIdx& v) {
   const int LD4 = g.LD >> 2, ix = v.ix, iz0 = v.iz0, fs = g.fs, NZ = g.NZ, NX = g.NX, L = g.L;
-  const size_t off = (size_t)v.s * g.FSZ;
-  const R* pb = PB + off;
-  R* ub = UB + off;
-  R* wb = WB + off;
   // ---- adjoint: u on ix in [2, NX-2], iz in [2, NZ-1]; w on ix in [2, NX-1], iz in [2, NZ-2]
-  if (ix >= 2 && ix <= NX - 1 && iz0 <= NZ - 1) {
+  if (FAST || (ix >= 2 && ix <= NX - 1 && iz0 <= NZ - 1)) {
     const V4<R> a = ld4(g.A, v.k4);
     const V4<R> p0 = ld4(pb, v.k4);
-    if (ix <= NX - 2) {
+    if (FAST || ix <= NX - 2) {
       V4<R> uv = ld4(ub, v.k4);
       const V4<R> pp1 = ld4(pb, v.k4 + LD4), pp2 = ld4(pb, v.k4 + 2 * LD4), pm1 = ld4(pb, v.k4 - LD4);
 #pragma unroll
       for (int j = 0; j < 4; ++j) {
         const int iz = iz0 + j;
-        if (iz >= 2 && iz <= NZ - 1) {
+        if (FAST || (iz >= 2 && iz <= NZ - 1)) {
           const R kappa = R(0.5) * (DAMPV(iz, ix) + DAMPV(iz, ix + 1)) * g.dt;
           uv.x[j] = (R(1.0) - kappa) * uv.x[j] - a.x[j] * (g.c1 * (pp1.x[j] - p0.x[j]) + g.c2 * (pp2.x[j] - pm1.x[j]));
         }
@@ -301,136 +329,113 @@ __global__ void __launch_bounds__(256) k_bwd_uw_v(Grid<R> g, const R* __restrict
     }
     V4<R> wv = ld4(wb, v.k4);
     R pz[7];  // pb at rows iz0-1 .. iz0+5
-    pz[1] = p0.x[0];
-    pz[2] = p0.x[1];
-    pz[3] = p0.x[2];
-    pz[4] = p0.x[3];
-    pz[0] = v.q > 0 ? pb[(size_t)(ix - 1) * g.LD + iz0 - 2] : R(0);
-    if (v.q + 1 < LD4) {
-      const V4<R> pn = ld4(pb, v.k4 + 1);
-      pz[5] = pn.x[0];
-      pz[6] = pn.x[1];
-    } else {
-      pz[5] = pz[6] = R(0);
-    }
+    col_window(pb, v, LD4, p0, pz, -1, 2);
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
       const int iz = iz0 + j;
-      if (iz >= 2 && iz <= NZ - 2) {
+      if (FAST || (iz >= 2 && iz <= NZ - 2)) {
         const R kappa = R(0.5) * (DAMPV(iz, ix) + DAMPV(iz + 1, ix)) * g.dt;
         wv.x[j] = (R(1.0) - kappa) * wv.x[j] - a.x[j] * (g.c1 * (pz[j + 2] - pz[j + 1]) + g.c2 * (pz[j + 3] - pz[j]));
       }
     }
-    // w(fs-1, ix) = w(fs, ix) for ix in [2, NX-1] (fdcore.f90:329-333).  When
-    // row fs-1 ends the vector above, the owner of row fs writes it and that
-    // vector's owner stores its other three rows.
-    const int jm = fs - 1 - iz0, jr = fs - iz0;
-    if (g.fs_flag == 1 && jr == 0) wb[(size_t)(ix - 1) * g.LD + (fs - 2)] = wv.x[0];
-    if (g.fs_flag == 1 && jm >= 0 && jm < 4) {
-      if (jr < 4) {
-        wv.x[jm] = wv.x[jr];
-        st4(wb, v.k4, wv);
-      } else {
-        st4_except(wb, v.k4, wv, jm);
-      }
-    } else {
+    if (FAST) {
       st4(wb, v.k4, wv);
+    } else {
+      // w(fs-1, ix) = w(fs, ix) for ix in [2, NX-1] (fdcore.f90:329-333).  When
+      // row fs-1 ends the vector above, the owner of row fs writes it and that
+      // vector's owner stores its other three rows.
+      const int jm = fs - 1 - iz0, jr = fs - iz0;
+      if (g.fs_flag == 1 && jr == 0) wb[(size_t)(ix - 1) * g.LD + (fs - 2)] = wv.x[0];
+      if (g.fs_flag == 1 && jm >= 0 && jm < 4) {
+        if (jr < 4) {
+          wv.x[jm] = wv.x[jr];
+          st4(wb, v.k4, wv);
+        } else {
+          st4_except(wb, v.k4, wv, jm);
+        }
+      } else {
+        st4(wb, v.k4, wv);
+      }
     }
   }
   // ---- reconstruction on the interior
   const int jx = ix - L, jz0 = iz0 - L;
-  if (jx < 1 || jx > g.nx || jz0 + 3 < 1 || jz0 > g.nz) return;
+  if (!FAST && (jx < 1 || jx > g.nx || jz0 + 3 < 1 || jz0 > g.nz)) return;
   const int nx = g.nx, nz = g.nz, fsi = fs - L;
-  const R* pe = PE + off;
-  R* ue = UE + off;
-  R* we = WE + off;
-  const R* b = strips + ((size_t)v.s * g.nt + (it - 2)) * g.SL;  // boundary(:, it-1)
-  const StripOff o = strip_offsets(nx, nz);
   const V4<R> bb = ld4(g.B, v.k4);
   const V4<R> e0 = ld4(pe, v.k4);
   V4<R> uv = ld4(ue, v.k4), wv = ld4(we, v.k4);
-  if (jx >= 2 && jx <= nx - 2) {
+  if (FAST || (jx >= 2 && jx <= nx - 2)) {
     const V4<R> ep1 = ld4(pe, v.k4 + LD4), ep2 = ld4(pe, v.k4 + 2 * LD4), em1 = ld4(pe, v.k4 - LD4);
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
       const int jz = jz0 + j;
-      if (jz >= fsi + 1 && jz <= nz - 1)
+      if (FAST || (jz >= fsi + 1 && jz <= nz - 1))
         uv.x[j] = uv.x[j] + bb.x[j] * (g.c1 * (ep1.x[j] - e0.x[j]) + g.c2 * (ep2.x[j] - em1.x[j]));
     }
   }
-  if (jx >= 2 && jx <= nx - 1) {
+  if (FAST || (jx >= 2 && jx <= nx - 1)) {
     R ez[7];  // pe at rows iz0-1 .. iz0+5 (zero outside the interior)
-    ez[1] = e0.x[0];
-    ez[2] = e0.x[1];
-    ez[3] = e0.x[2];
-    ez[4] = e0.x[3];
-    ez[0] = v.q > 0 ? pe[(size_t)(ix - 1) * g.LD + iz0 - 2] : R(0);
-    if (v.q + 1 < LD4) {
-      const V4<R> en = ld4(pe, v.k4 + 1);
-      ez[5] = en.x[0];
-      ez[6] = en.x[1];
-    } else {
-      ez[5] = ez[6] = R(0);
-    }
+    col_window(pe, v, LD4, e0, ez, -1, 2);
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
       const int jz = jz0 + j;
-      if (jz >= fsi + 1 && jz <= nz - 2)
+      if (FAST || (jz >= fsi + 1 && jz <= nz - 2))
         wv.x[j] = wv.x[j] + bb.x[j] * (g.c1 * (ez[j + 2] - ez[j + 1]) + g.c2 * (ez[j + 3] - ez[j]));
     }
   }
+  if (!FAST) {
+    const R* b = strips + ((size_t)v.s * g.nt + (it - 2)) * g.SL;  // boundary(:, it-1)
+    const StripOff o = strip_offsets(nx, nz);
 #pragma unroll
-  for (int j = 0; j < 4; ++j) {
-    const int jz = jz0 + j;
-    if (jz < 1 || jz > nz) continue;
-    if (jz == nz - 1) wv.x[j] = b[o.B2 + jx - 1];
-    if (jx == 1) uv.x[j] = b[o.S2 + jz - 1];
-    if (jx == nx - 1) uv.x[j] = b[o.S5 + jz - 1];
+    for (int j = 0; j < 4; ++j) {
+      const int jz = jz0 + j;
+      if (jz < 1 || jz > nz) continue;
+      if (jz == nz - 1) wv.x[j] = b[o.B2 + jx - 1];
+      if (jx == 1) uv.x[j] = b[o.S2 + jz - 1];
+      if (jx == nx - 1) uv.x[j] = b[o.S5 + jz - 1];
+    }
   }
   st4(ue, v.k4, uv);
   st4(we, v.k4, wv);
 }
 
+template <class R>
+__global__ void __launch_bounds__(256) k_bwd_uw_v(Grid<R> g, const R* __restrict__ PB, R* UB, R* WB,
+                                                  const R* __restrict__ PE, R* UE, R* WE,
+                                                  const R* __restrict__ strips, int it, int shot0) {
+  const VecIdx v = vec_index(g, shot0);
+  if (!v.ok) return;
+  const size_t off = (size_t)v.s * g.FSZ;
+  if (v.deep)
+    bwd_uw_body<R, true>(g, PB + off, UB + off, WB + off, PE + off, UE + off, WE + off, strips, it, v);
+  else
+    bwd_uw_body<R, false>(g, PB + off, UB + off, WB + off, PE + off, UE + off, WE + off, strips, it, v);
+}
+
+// ---------------------------------------------------------------------------
 // Backward pressure phase: adjoint p + injection + mirror (fdcore.f90:336-373),
 // reconstruction p with source subtraction and re-insert (fdcore.f90:249-287),
 // imaging sums (solver.f90:237-239).
-template <class R>
-__global__ void __launch_bounds__(256) k_bwd_p_v(Grid<R> g, Receivers rec, Sources src, const R* __restrict__ s_fwd,
-                                                 const R* __restrict__ adj_t, R* PB, const R* __restrict__ UB,
-                                                 const R* __restrict__ WB, R* PE, const R* __restrict__ UE,
-                                                 const R* __restrict__ WE, R* DG, R* DFW, R* DBK,
-                                                 const R* __restrict__ strips, int it, int shot0) {
-  const VecIdx v = vec_index(g, shot0);
-  if (!v.ok) return;
+template <class R, bool FAST>
+__device__ __forceinline__ void bwd_p_body(const Grid<R>& g, const Receivers& rec, const Sources& src,
+                                           const R* __restrict__ s_fwd, const R* __restrict__ adj_t, R* __restrict__ pb,
+                                           const R* __restrict__ ub, const R* __restrict__ wb, R* __restrict__ pe,
+                                           const R* __restrict__ ue, const R* __restrict__ we, R* __restrict__ dg, R* __restrict__ dfw, R* __restrict__ dbk,
+                                           const R* __restrict__ strips, int it, const VecIdx& v) {
   const int LD4 = g.LD >> 2, ix = v.ix, iz0 = v.iz0, fs = g.fs, NZ = g.NZ, NX = g.NX, L = g.L;
-  const size_t off = (size_t)v.s * g.FSZ;
-  R* pb = PB + off;
-  const R* ub = UB + off;
-  const R* wb = WB + off;
   const V4<R> pold = ld4(pb, v.k4);
   V4<R> pv = pold;
   bool dirty = false;
-  if (ix >= 3 && ix <= NX - 2 && iz0 + 3 >= 3 && iz0 <= NZ - 2) {
+  if (FAST || (ix >= 3 && ix <= NX - 2 && iz0 + 3 >= 3 && iz0 <= NZ - 2)) {
     const V4<R> bcoef = ld4(g.B, v.k4);
     const V4<R> u0 = ld4(ub, v.k4), um1 = ld4(ub, v.k4 - LD4), up1 = ld4(ub, v.k4 + LD4), um2 = ld4(ub, v.k4 - 2 * LD4);
     R wz[7];  // wb at rows iz0-2 .. iz0+4
-    const V4<R> w0 = ld4(wb, v.k4);
-    wz[2] = w0.x[0];
-    wz[3] = w0.x[1];
-    wz[4] = w0.x[2];
-    wz[5] = w0.x[3];
-    if (v.q > 0) {
-      const V4<R> wm = ld4(wb, v.k4 - 1);
-      wz[0] = wm.x[2];
-      wz[1] = wm.x[3];
-    } else {
-      wz[0] = wz[1] = R(0);
-    }
-    wz[6] = (v.q + 1 < LD4) ? wb[(size_t)(ix - 1) * g.LD + iz0 + 3] : R(0);
+    col_window(wb, v, LD4, ld4(wb, v.k4), wz, -2, 1);
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
       const int iz = iz0 + j;
-      if (iz >= 3 && iz <= NZ - 2) {
+      if (FAST || (iz >= 3 && iz <= NZ - 2)) {
         const R kappa = DAMPV(iz, ix) * g.dt;
         pv.x[j] = (R(1.0) - kappa) * pv.x[j] -
                   bcoef.x[j] * (g.c1 * (u0.x[j] - um1.x[j] + wz[j + 2] - wz[j + 1]) +
@@ -439,88 +444,78 @@ __global__ void __launch_bounds__(256) k_bwd_p_v(Grid<R> g, Receivers rec, Sourc
     }
     dirty = true;
   }
-  if (iz0 + 3 >= rec.zlo[v.s] && iz0 <= rec.zhi[v.s]) {
-    const int* cp = rec.colptr + (size_t)v.s * (NX + 2);
-    const int e1 = cp[ix + 1];
-    for (int e = cp[ix]; e < e1; ++e) {
-      const int j = rec.zrow[e] - iz0;
-      if (j >= 0 && j < 4) {
-        pv.x[j] = pv.x[j] + g.dt * adj_t[((size_t)v.s * g.nt + (it - 1)) * g.ngmax + rec.ig[e]];
-        dirty = true;
+  if (FAST) {
+    st4(pb, v.k4, pv);
+  } else {
+    if (iz0 + 3 >= rec.zlo[v.s] && iz0 <= rec.zhi[v.s]) {
+      const int* cp = rec.colptr + (size_t)v.s * (NX + 2);
+      const int e1 = cp[ix + 1];
+      for (int e = cp[ix]; e < e1; ++e) {
+        const int j = rec.zrow[e] - iz0;
+        if (j >= 0 && j < 4) {
+          pv.x[j] = pv.x[j] + g.dt * adj_t[((size_t)v.s * g.nt + (it - 1)) * g.ngmax + rec.ig[e]];
+          dirty = true;
+        }
       }
     }
-  }
-  // p(fs-1, ix) = -p(fs+1, ix) for every column (fdcore.f90:370-373).  When
-  // row fs-1 lies in the vector above, the owner of row fs+1 writes it and
-  // that vector's owner stores its other rows.
-  const int jm = fs - 1 - iz0, jp = fs + 1 - iz0;
-  if (jp >= 0 && jp < 4 && jm < 0) pb[(size_t)(ix - 1) * g.LD + (fs - 2)] = -pv.x[jp];
-  if (jm >= 0 && jm < 4) {
-    if (jp < 4) {
-      pv.x[jm] = -pv.x[jp];
+    // p(fs-1, ix) = -p(fs+1, ix) for every column (fdcore.f90:370-373).  When
+    // row fs-1 lies in the vector above, the owner of row fs+1 writes it and
+    // that vector's owner stores its other rows.
+    const int jm = fs - 1 - iz0, jp = fs + 1 - iz0;
+    if (jp >= 0 && jp < 4 && jm < 0) pb[(size_t)(ix - 1) * g.LD + (fs - 2)] = -pv.x[jp];
+    if (jm >= 0 && jm < 4) {
+      if (jp < 4) {
+        pv.x[jm] = -pv.x[jp];
+        st4(pb, v.k4, pv);
+      } else {
+        st4_except(pb, v.k4, pv, jm);
+      }
+    } else if (dirty) {
       st4(pb, v.k4, pv);
-    } else {
-      st4_except(pb, v.k4, pv, jm);
     }
-  } else if (dirty) {
-    st4(pb, v.k4, pv);
   }
 
   // ---- reconstruction p, re-insert, imaging on the interior
   const int jx = ix - L, jz0 = iz0 - L;
-  if (jx < 1 || jx > g.nx || jz0 + 3 < 1 || jz0 > g.nz) return;
+  if (!FAST && (jx < 1 || jx > g.nx || jz0 + 3 < 1 || jz0 > g.nz)) return;
   const int nx = g.nx, nz = g.nz, fsi = fs - L;
-  R* pe = PE + off;
-  const R* ue = UE + off;
-  const R* we = WE + off;
-  const R* b = strips + ((size_t)v.s * g.nt + (it - 2)) * g.SL;
-  const StripOff o = strip_offsets(nx, nz);
   V4<R> ev = ld4(pe, v.k4);
-  const int rj = src.risz[v.s] - jz0;
-  if (jx == src.risx[v.s] && rj >= 0 && rj < 4) ev.x[rj] = ev.x[rj] - g.dt * s_fwd[(size_t)v.s * (g.nt + 1) + it];
-  if (jx >= 3 && jx <= nx - 2) {
+  if (!FAST) {
+    const int rj = src.risz[v.s] - jz0;
+    if (jx == src.risx[v.s] && rj >= 0 && rj < 4) ev.x[rj] = ev.x[rj] - g.dt * s_fwd[(size_t)v.s * (g.nt + 1) + it];
+  }
+  if (FAST || (jx >= 3 && jx <= nx - 2)) {
     const V4<R> a = ld4(g.A, v.k4);
     const V4<R> u0 = ld4(ue, v.k4), um1 = ld4(ue, v.k4 - LD4), up1 = ld4(ue, v.k4 + LD4), um2 = ld4(ue, v.k4 - 2 * LD4);
-    R wz[7];
-    const V4<R> w0 = ld4(we, v.k4);
-    wz[2] = w0.x[0];
-    wz[3] = w0.x[1];
-    wz[4] = w0.x[2];
-    wz[5] = w0.x[3];
-    if (v.q > 0) {
-      const V4<R> wm = ld4(we, v.k4 - 1);
-      wz[0] = wm.x[2];
-      wz[1] = wm.x[3];
-    } else {
-      wz[0] = wz[1] = R(0);
-    }
-    wz[6] = (v.q + 1 < LD4) ? we[(size_t)(ix - 1) * g.LD + iz0 + 3] : R(0);
+    R wz[7];  // we at rows iz0-2 .. iz0+4
+    col_window(we, v, LD4, ld4(we, v.k4), wz, -2, 1);
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
       const int jz = jz0 + j;
-      if (jz >= fsi + 2 && jz <= nz - 2)
+      if (FAST || (jz >= fsi + 2 && jz <= nz - 2))
         ev.x[j] = ev.x[j] + a.x[j] * (g.c1 * (u0.x[j] - um1.x[j] + wz[j + 2] - wz[j + 1]) +
                                       g.c2 * (up1.x[j] - um2.x[j] + wz[j + 3] - wz[j]));
     }
   }
-  R* dg = DG + off;
-  R* dfw = DFW + off;
-  R* dbk = DBK + off;
   V4<R> g0 = ld4(dg, v.k4), f0 = ld4(dfw, v.k4), k0 = ld4(dbk, v.k4);
+  const R* b = FAST ? nullptr : strips + ((size_t)v.s * g.nt + (it - 2)) * g.SL;
+  const StripOff o = strip_offsets(nx, nz);
 #pragma unroll
   for (int j = 0; j < 4; ++j) {
     const int jz = jz0 + j;
-    if (jz < 1 || jz > nz) continue;
+    if (!FAST && (jz < 1 || jz > nz)) continue;
     R pf = ev.x[j];
-    if (jz == nz) pf = b[o.B0 + jx - 1];
-    if (jz == nz - 1) pf = b[o.B1 + jx - 1];
-    if (jx == 1) pf = b[o.S0 + jz - 1];
-    if (jx == 2) pf = b[o.S1 + jz - 1];
-    if (jx == nx) pf = b[o.S3 + jz - 1];
-    if (jx == nx - 1) pf = b[o.S4 + jz - 1];
-    if (jz == fsi) pf = b[o.T0 + jx - 1];
-    if (jz == fsi + 1) pf = b[o.T1 + jx - 1];
-    if (jz == fsi + 2) pf = b[o.T2 + jx - 1];
+    if (!FAST) {
+      if (jz == nz) pf = b[o.B0 + jx - 1];
+      if (jz == nz - 1) pf = b[o.B1 + jx - 1];
+      if (jx == 1) pf = b[o.S0 + jz - 1];
+      if (jx == 2) pf = b[o.S1 + jz - 1];
+      if (jx == nx) pf = b[o.S3 + jz - 1];
+      if (jx == nx - 1) pf = b[o.S4 + jz - 1];
+      if (jz == fsi) pf = b[o.T0 + jx - 1];
+      if (jz == fsi + 1) pf = b[o.T1 + jx - 1];
+      if (jz == fsi + 2) pf = b[o.T2 + jx - 1];
+    }
     ev.x[j] = pf;
     g0.x[j] = g0.x[j] + pf * (pold.x[j] - pv.x[j]);
     f0.x[j] = f0.x[j] + pf * pf;
@@ -530,6 +525,26 @@ __global__ void __launch_bounds__(256) k_bwd_p_v(Grid<R> g, Receivers rec, Sourc
   st4(dg, v.k4, g0);
   st4(dfw, v.k4, f0);
   st4(dbk, v.k4, k0);
+}
+
+template <class R>
+__global__ void __launch_bounds__(256) k_bwd_p_v(Grid<R> g, Receivers rec, Sources src, const R* __restrict__ s_fwd,
+                                                 const R* __restrict__ adj_t, R* PB, const R* __restrict__ UB,
+                                                 const R* __restrict__ WB, R* PE, const R* __restrict__ UE,
+                                                 const R* __restrict__ WE, R* DG, R* DFW, R* DBK,
+                                                 const R* __restrict__ strips, int it, int shot0) {
+  const VecIdx v = vec_index(g, shot0);
+  if (!v.ok) return;
+  const size_t off = (size_t)v.s * g.FSZ;
+  const bool rec_here = v.iz0 + 3 >= rec.zlo[v.s] && v.iz0 <= rec.zhi[v.s];
+  const int rz = src.risz[v.s] + g.L;  // reconstruction source row on the PML grid (risx = 0: none)
+  const bool src_here = src.risx[v.s] + g.L == v.ix && rz >= v.iz0 && rz < v.iz0 + 4;
+  if (v.deep && !rec_here && !src_here)
+    bwd_p_body<R, true>(g, rec, src, s_fwd, adj_t, PB + off, UB + off, WB + off, PE + off, UE + off, WE + off,
+                        DG + off, DFW + off, DBK + off, strips, it, v);
+  else
+    bwd_p_body<R, false>(g, rec, src, s_fwd, adj_t, PB + off, UB + off, WB + off, PE + off, UE + off, WE + off,
+                         DG + off, DFW + off, DBK + off, strips, it, v);
 }
 
 }  // namespace swit

@@ -163,6 +163,13 @@ class Engine:
         _lib.check(self._lib.swit_export_snapshot(self._h, b.ctypes.data, *[x.ctypes.data for x in ends], 0, None))
         return dict(boundary=b, p_end=ends[0], u_end=ends[1], w_end=ends[2])
 
+    def import_snapshot(self, src, boundary, p_end, u_end, w_end):
+        """Loads a saved forward run (see swit_import_snapshot): src (ns, nt), boundary
+        (ns, nt, 9nx+6nz), p_end/u_end/w_end (ns, nx, nz), all float32 host arrays."""
+        arrs = [self._f32(a) for a in (src, boundary, p_end, u_end, w_end)]
+        ptrs = [self._ptr(a, np.float32)[0] for a in arrs]
+        _lib.check(self._lib.swit_import_snapshot(self._h, *ptrs, 0, None))
+
     def profile_kernels(self):
         """Mean launch duration (ms) and launch count of the four stencil kernels,
         timed with CUDA events on torch's current stream (see swit_profile_kernels)."""

@@ -1,0 +1,97 @@
+"""Gradient preconditioning of SWIT on device (torch, float64), equal to the
+reference's numpy/scipy code:
+
+    grad_precond(grad, forw, back, ...)   toolbox/postprocess.py:20-85
+    grad_taper(nx, nz, ...)               toolbox/postprocess.py:88-111
+    smooth2d(Z, span)                     toolbox/tools.py:255-275 (Gaussian kernel of gauss2, 237-252)
+
+Arrays are (nx, nz) like the reference's; vectors of length nx*nz are reshaped.
+The figure the reference draws of the illuminations is not reproduced.
+"""
+import math
+
+import torch
+import torch.nn.functional as F
+
+
+def _gauss_kernel(span, dtype, device):
+    """tools.py:255-269: exp(-x^2/(2 span^2) - y^2/(2 span^2)) / (2 pi span^2) on
+    x, y = linspace(-2 span, 2 span, 2 span + 1), normalised to sum 1."""
+    x = torch.linspace(-2.0 * span, 2.0 * span, 2 * span + 1, dtype=torch.float64, device=device)
+    X, Y = torch.meshgrid(x, x, indexing="xy")
+    s2 = float(span) ** 2
+    Z = torch.exp(-0.5 * (X ** 2 / s2 + Y ** 2 / s2)) * (2.0 * math.pi * math.sqrt(s2 * s2)) ** -1.0
+    return (Z / Z.sum()).to(dtype)
+
+
+def _conv_same(Z, K):
+    """scipy.signal.convolve2d(Z, K, 'same') with zero fill (K has odd sides)."""
+    kh, kw = K.shape
+    out = F.conv2d(Z[None, None], torch.flip(K, (0, 1))[None, None], padding=(kh // 2, kw // 2))
+    return out[0, 0]
+
+
+def smooth2d(Z, span=10):
+    """tools.py:255-275: Gaussian smoothing, normalised by the smoothed ones array."""
+    Z = torch.as_tensor(Z, dtype=torch.float64)
+    K = _gauss_kernel(int(span), Z.dtype, Z.device)
+    # meshgrid(x, y) in the reference puts x along columns: K[i, j] = f(y_i, x_j), symmetric anyway
+    num = _conv_same(Z, K)
+    den = _conv_same(torch.ones_like(Z), K)
+    return num / den
+
+
+def _hamming(M, dtype, device):
+    n = torch.arange(M, dtype=torch.float64, device=device)
+    return (0.54 - 0.46 * torch.cos(2.0 * math.pi * n / (M - 1))).to(dtype)
+
+
+def grad_taper(nx, nz, tapersize=20, thred=0.05, marine_or_land="Marine", device="cpu"):
+    """postprocess.py:88-111 (the Marine/Offshore test is case-sensitive, as there)."""
+    if marine_or_land in ["Marine", "Offshore"]:
+        taper = torch.ones((nx, nz), dtype=torch.float64, device=device)
+        taper[:, :tapersize] = 0.0
+        return taper
+    H = _hamming(tapersize * 2, torch.float64, device)[tapersize:]
+    taper = torch.zeros((nx, nz), dtype=torch.float64, device=device)
+    taper[:, :tapersize] = H
+    taper = smooth2d(taper, span=tapersize // 2)
+    taper = taper / taper.max()
+    taper = taper * (1 - thred)
+    taper = -taper + 1
+    return taper * taper
+
+
+def grad_precond(grad, forw, back, nx, nz, vpmax, marine_or_land, grad_mute, grad_thred, grad_smooth,
+                 grad_mask=None):
+    """postprocess.py:20-85: taper, illumination (pseudo-Hessian) preconditioning,
+    optional smoothing and mask, scaling to vpmax / max|g|.  Returns a vector of nx*nz."""
+    dev = grad.device if torch.is_tensor(grad) else "cpu"
+    grad = torch.as_tensor(grad, dtype=torch.float64, device=dev).reshape(nx, nz).clone()
+    forw = torch.as_tensor(forw, dtype=torch.float64, device=dev).reshape(nx, nz)
+    back = torch.as_tensor(back, dtype=torch.float64, device=dev).reshape(nx, nz)
+    if grad_mute > 0:
+        grad = grad * grad_taper(nx, nz, tapersize=grad_mute, thred=grad_thred, marine_or_land=marine_or_land,
+                                 device=dev)
+    span = 40 if min(nx, nz) > 40 else int(min(nx, nz) / 2)
+    forw = smooth2d(forw, span)
+    back = smooth2d(back, span)
+    epsilon = 0.0001
+    forw = forw / forw.max()
+    back = back / back.max()
+    precond = forw + back
+    precond = precond / precond.max()
+    precond = torch.where(precond < epsilon, torch.full_like(precond, epsilon), precond)
+    grad = grad / precond
+    if grad_smooth > 0:
+        if marine_or_land in ["Marine", "Offshore"]:
+            grad[:, grad_mute:] = smooth2d(grad[:, grad_mute:], span=grad_smooth)
+        else:
+            grad = smooth2d(grad, span=grad_smooth)
+    if grad_mask is not None:
+        mask = torch.as_tensor(grad_mask, dtype=torch.float64, device=dev)
+        if tuple(mask.shape) != (nx, nz):
+            raise ValueError("Wrong size of grad mask: the size of the mask should be identical to the size of vp model")
+        grad = grad * mask
+    grad = grad * (vpmax / grad.abs().max())
+    return grad.reshape(nx * nz)

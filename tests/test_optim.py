@@ -1,0 +1,57 @@
+"""The device optimiser against search directions made by the reference's own
+toolbox/inversion.py (tests/golden/make_optim_golden.py), on CPU tensors; the
+same torch code runs on the GPU."""
+import importlib.util
+import os
+
+import numpy as np
+import pytest
+import torch
+
+from swit_gb300 import optim as O
+
+G = np.load(os.path.join(os.path.dirname(__file__), "golden", "optim_golden.npz"))
+_spec = importlib.util.spec_from_file_location("_mk", os.path.join(os.path.dirname(__file__), "golden",
+                                                                   "make_optim_golden.py"))
+_mk = importlib.util.module_from_spec(_spec)
+_spec.loader.exec_module(_mk)
+
+
+@pytest.mark.parametrize("scheme,key", [("LBFGS", "d_lbfgs"), ("NLCG", "d_nlcg")])
+def test_directions_match_reference(scheme, key):
+    A, b, v0 = _mk.problem()
+    A, b = torch.from_numpy(A), torch.from_numpy(b)
+    st = O.init_state(scheme, v0.size, device="cpu")
+    st["v_now"] = torch.from_numpy(v0.copy())
+    st["v_old"] = torch.from_numpy(v0.copy())
+    for i in range(4):
+        st["g_now"] = A @ st["v_now"] - b
+        st = O.nlcg_direction(st) if scheme == "NLCG" else O.lbfgs_direction(st)
+        ref = G[key][i]
+        np.testing.assert_allclose(st["d_now"].numpy(), ref, rtol=0, atol=2e-5 * np.abs(ref).max())
+        if scheme == "NLCG":
+            st["g_old"], st["d_old"] = st["g_now"], st["d_now"]
+        else:
+            st["g_old"], st["v_old"] = st["g_now"], st["v_now"]
+        st["v_now"] = st["v_now"] + 0.5 * st["d_now"]
+
+
+@pytest.mark.parametrize("scheme", ["LBFGS", "NLCG"])
+def test_fwi_loop_decreases_a_quadratic(scheme):
+    A, b, v0 = _mk.problem()
+    A, b = torch.from_numpy(A), torch.from_numpy(b)
+
+    def f(v):
+        return 0.5 * v @ (A @ v) - b @ v
+
+    st, hist = O.fwi(torch.from_numpy(v0), lambda v: (f(v), A @ v - b), f, scheme=scheme, maxiter=5,
+                     step_length=0.5, vpmax=1e9, vpmin=-1e9)
+    fs = [h["f"] for h in hist]
+    assert all(h["ls_status"] == 0 for h in hist)
+    assert fs == sorted(fs, reverse=True) and fs[-1] < float(f(torch.from_numpy(v0)))
+
+
+def test_model_update_clips_to_bounds():
+    v = torch.tensor([1000.0, 2000.0, 4900.0])
+    out = O.model_update(v, torch.tensor([-500.0, 10.0, 500.0]), 5000.0, 1000.0)
+    assert out.tolist() == [1000.0, 2010.0, 5000.0]
