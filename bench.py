@@ -102,7 +102,7 @@ def ncu_traffic():
         for line in open(p):
             if line.startswith("traffic "):
                 kv = dict(x.split("=", 1) for x in line.split()[1:])
-                out[kv["kernel"]] = float(kv["bytes_per_shot_launch"])
+                out[(kv["kernel"], kv.get("variant"))] = float(kv["bytes_per_shot_launch"])
     return out
 
 
@@ -340,7 +340,7 @@ def run_mine(args):
         top = max(tot, key=tot.get)
         alg = kb[top] * shots_launch
         achieved = alg / (prof[top]["mean_ms"] / 1000.0) / 1e9
-        traffic = ncu_traffic().get(top)
+        traffic = ncu_traffic().get((top, q["kernel"]))
         line["roofline"] = {"bound": "hbm", "kernel": top, "achieved": achieved, "peak": peak, "unit": "GB/s",
                             "frac": achieved / peak, "peak_kind": peak_kind,
                             "traffic": traffic * shots_launch if traffic else None,
