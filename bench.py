@@ -43,7 +43,7 @@ def parse():
     ap.add_argument("--nt", type=int, default=None, help="time steps (default 4000)")
     ap.add_argument("--batch", type=int, default=0, help="shots per launch (0 = engine default)")
     ap.add_argument("--block-x", type=int, default=0)
-    ap.add_argument("--kernel", default="auto", choices=["auto", "fused", "split", "vec"])
+    ap.add_argument("--kernel", default="auto", choices=["auto", "fused", "split", "vec", "cluster"])
     ap.add_argument("--no-tune", action="store_true", help="skip the launch-configuration autotuner")
     ap.add_argument("--no-extras", action="store_true", help="skip plain path, CPU baseline and kernel profile")
     return ap.parse_args()
@@ -67,12 +67,13 @@ def work_units(nx, nz, npml, nt, ng):
     return U, B
 
 
-def kernel_bytes_per_shot(nx, nz, npml, ng):
+def kernel_bytes_per_shot(nx, nz, npml, ng, nt):
     """Compulsory bytes one launch of each stencil kernel moves per shot (each
-    array it touches read or written once, neighbours not counted again)."""
+    array it touches read or written once per time step, neighbours not counted
+    again).  The cluster kernels run the whole time loop in one launch."""
     npts = (nx + 2 * npml) * (nz + 2 * npml)
     nint = nx * nz
-    return {
+    step = {
         "fwd_p": 20 * npts,                                   # p r/w, u, w, A
         "fwd_uw": 24 * npts + 4 * (9 * nx + 6 * nz) + 4 * ng,  # u, w r/w, p, B; strips, trace samples
         "bwd_uw": 24 * npts + 24 * nint + 4 * (nx + 2 * nz),   # adjoint u, w; reconstruction u, w; strips
@@ -82,6 +83,9 @@ def kernel_bytes_per_shot(nx, nz, npml, ng):
         "fwd_step": 32 * npts + 4 * (9 * nx + 6 * nz) + 4 * ng,
         "bwd_step": 32 * npts + 48 * nint + 4 * (6 * nx + 6 * nz) + 4 * ng,
     }
+    step["fwd_loop"] = (nt - 1) * (step["fwd_p"] + step["fwd_uw"])
+    step["bwd_loop"] = (nt - 1) * (step["bwd_uw"] + step["bwd_p"])
+    return step
 
 
 def measured_peak():
@@ -334,7 +338,7 @@ def run_mine(args):
     if not args.no_extras:
         # per-kernel launch durations (CUDA events around every launch)
         prof = eng.profile_kernels()
-        kb = kernel_bytes_per_shot(sv.nx, sv.nz, sv.npml, sv.ng)
+        kb = kernel_bytes_per_shot(sv.nx, sv.nz, sv.npml, sv.ng, sv.nt)
         shots_launch = q["shots_per_batch"]
         tot = {k: v["launches"] * v["mean_ms"] for k, v in prof.items()}
         top = max(tot, key=tot.get)

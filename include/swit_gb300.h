@@ -72,11 +72,18 @@ typedef struct swit_desc {
   int32_t block_x;          /* columns per CTA, 0 = automatic: split kernels
                                1, 2, 4 or 8 (x 32 rows); fused kernels 8, 16
                                or 32 (x all rows); vec kernels 4..64 columns x
-                               256/block_x four-row vectors (default 32)         */
+                               256/block_x four-row vectors (default 32);
+                               cluster kernels: CTAs per cluster 1..16 (default
+                               16; the reverse loop takes more CTAs when its six
+                               wavefields need them)                            */
   int32_t kernel_variant;   /* 0 = automatic (vec), 1 = split: two kernels per step,
                                in place, one point per thread; 2 = fused: one
                                kernel per step, double-buffered (NZ + 2 npml <=
-                               1024); 3 = vec: split, four rows per thread      */
+                               1024); 3 = vec: split, four rows per thread;
+                               4 = cluster: one launch per time loop, one
+                               thread-block cluster per shot holding its
+                               wavefields in distributed shared memory
+                               (SWIT_E_LIMIT when they do not fit)              */
 } swit_desc;
 
 /* Creates an engine and allocates its device workspace on the current device.

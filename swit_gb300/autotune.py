@@ -10,6 +10,7 @@ import time
 
 import numpy as np
 
+from ._lib import SwitError
 from .engine import Engine
 
 _cache = {}
@@ -29,6 +30,8 @@ def candidates(ns, nz_pml):
         for b in batches:
             out.append(dict(kernel="vec", block_x=bx, shots_per_batch=b))
     out.append(dict(kernel="split", block_x=4, shots_per_batch=ns))
+    for cl in (16, 8):
+        out.append(dict(kernel="cluster", block_x=cl, shots_per_batch=ns))
     return out
 
 
@@ -48,7 +51,13 @@ def tune(nx, nz, npml, dx, dt, src_xz, rec_xz, vp, rho, free_surface=1, trial_st
     src = torch.from_numpy(rng.standard_normal((ns, nt)).astype(np.float32)).cuda()
     times = []
     for c in cands:
-        with Engine(nx, nz, npml, nt, dx, dt, src_xz, rec_xz, free_surface=free_surface, **c) as e:
+        try:
+            eng = Engine(nx, nz, npml, nt, dx, dt, src_xz, rec_xz, free_surface=free_surface, **c)
+        except SwitError as err:  # e.g. a cluster variant whose wavefields do not fit on chip
+            if verbose:
+                print("autotune", c, "unavailable:", err)
+            continue
+        with eng as e:
             e.set_model(vp, rho)
             obs = torch.zeros((ns, e.ngmax, nt), dtype=torch.float32, device="cuda")
             e.gradient_l2(src, obs)  # graphs captured here

@@ -47,5 +47,5 @@ def build(force: bool = False, verbose: bool = False, extra=()) -> str:
 
 
 if __name__ == "__main__":
-    extra = [a for a in sys.argv[1:] if a.startswith("-X")]
+    extra = [a for a in sys.argv[1:] if a.startswith(("-X", "-D"))]
     print(build(force=True, verbose=True, extra=extra))

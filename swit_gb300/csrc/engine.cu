@@ -18,6 +18,7 @@
 #include "kernels.cuh"
 #include "kernels_fused.cuh"
 #include "kernels_vec.cuh"
+#include "kernels_cluster.cuh"
 
 using namespace swit;
 
@@ -55,7 +56,11 @@ struct swit_engine {
   int nx, nz, L, nt, NX, NZ, LD, LDI, fs, fs_flag, ns, ngmax, SL, prec, path;
   float dx32, dt32;
   int batch, bx;
-  int variant;  // 1 = split, 2 = fused (one kernel per step, ping-pong), 3 = vec (split, 4 rows per thread)
+  int variant;  // 1 = split, 2 = fused (one kernel per step, ping-pong), 3 = vec (split, 4 rows per thread),
+                // 4 = cluster (one persistent cluster per shot, wavefields in distributed shared memory)
+  // cluster variant: cluster sizes, threads per CTA, A and B on chip, dynamic shared memory
+  int clf = 0, clb = 0, maxt = 0, ab_local = 0;
+  size_t smf = 0, smb = 0;
   int IL;       // interior fields: row/column offset into their layout (npml for vec, else 0)
   int device;
   size_t esz;  // sizeof(R)
@@ -66,6 +71,7 @@ struct swit_engine {
   double* d_mtrace = nullptr;
   // device arrays of type R (float or double)
   void *A = nullptr, *B = nullptr, *damp = nullptr, *cint = nullptr;
+  void *kp = nullptr, *ku = nullptr, *kw = nullptr;  // damping factors per point (vec and cluster kernels)
   void *p = nullptr, *u = nullptr, *w = nullptr, *pb = nullptr, *ub = nullptr, *wb = nullptr;
   void *pe = nullptr, *ue = nullptr, *we = nullptr, *dg = nullptr, *dfw = nullptr, *dbk = nullptr;
   void *strips = nullptr, *src = nullptr, *seis_t = nullptr, *adj_t = nullptr;
@@ -113,7 +119,7 @@ void release(swit_engine* e) {
   if (e->gbwd) cudaGraphExecDestroy(e->gbwd);
   if (e->cap) cudaStreamDestroy(e->cap);
   void* ptrs[] = {e->d_zlo, e->d_zhi, e->d_ng, e->d_isx, e->d_isz, e->d_risx, e->d_risz, e->d_colptr, e->d_ig, e->d_zr, e->d_live,
-                  e->d_mtrace, e->A, e->B, e->damp, e->cint, e->p, e->u, e->w, e->pb, e->ub, e->wb, e->pe,
+                  e->d_mtrace, e->A, e->B, e->damp, e->cint, e->kp, e->ku, e->kw, e->p, e->u, e->w, e->pb, e->ub, e->wb, e->pe,
                   e->ue, e->we, e->dg, e->dfw, e->dbk, e->strips, e->src, e->seis_t, e->adj_t, e->d_in,
                   e->d_stage, e->p2, e->u2, e->w2, e->pb2, e->ub2, e->wb2, e->pe2, e->ue2, e->we2};
   for (void* q : ptrs)
@@ -136,15 +142,18 @@ Grid<R> make_grid(const swit_engine* e) {
   g.ngmax = e->ngmax;
   g.SL = e->SL;
   g.FSZ = (size_t)e->NX * e->LD;
-  g.FSI = e->variant == 3 ? g.FSZ : (size_t)e->nx * e->LDI;
+  g.FSI = e->variant >= 3 ? g.FSZ : (size_t)e->nx * e->LDI;
   g.IL = e->IL;
-  if (e->variant == 3) g.LDI = e->LD;
+  if (e->variant >= 3) g.LDI = e->LD;
   g.dt = (R)e->dt32;
   g.c1 = R(9.0) / R(8.0);    // global.f90:34
   g.c2 = R(-1.0) / R(24.0);  // global.f90:35
   g.A = (const R*)e->A;
   g.B = (const R*)e->B;
   g.damp = (const R*)e->damp;
+  g.kp = (const R*)e->kp;
+  g.ku = (const R*)e->ku;
+  g.kw = (const R*)e->kw;
   return g;
 }
 
@@ -224,9 +233,52 @@ inline dim3 vec_grid(const swit_engine* e, int nb) {
   return dim3((e->LD / 4 + vz - 1) / vz, (e->NX + e->bx - 1) / e->bx, nb);
 }
 
+// Cluster variant: one launch runs the whole time loop of nb shots, one
+// cluster of e->clf (forward) or e->clb (reverse) CTAs per shot.
+inline cudaLaunchConfig_t cluster_config(int C, int nb, int threads, size_t smem, cudaStream_t st,
+                                         cudaLaunchAttribute* at) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(C, nb, 1);
+  cfg.blockDim = dim3(threads, 1, 1);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  at[0].id = cudaLaunchAttributeClusterDimension;
+  at[0].val.clusterDim.x = C;
+  at[0].val.clusterDim.y = 1;
+  at[0].val.clusterDim.z = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  return cfg;
+}
+
+template <class R, int MAXT>
+void launch_cluster_fwd_t(swit_engine* e, bool store, int shot0, int nb, cudaStream_t st) {
+  cudaLaunchAttribute at[1];
+  const cudaLaunchConfig_t cfg = cluster_config(e->clf, nb, e->maxt, e->smf, st, at);
+  R* strips = store ? (R*)e->strips : nullptr;
+  cudaLaunchKernelEx(&cfg, k_fwd_cl<R, MAXT>, make_grid<R>(e), make_src(e), make_rec(e), (const R*)e->src, (R*)e->p,
+                     (R*)e->u, (R*)e->w, (R*)e->seis_t, strips, shot0, e->ab_local);
+}
+
+template <class R, int MAXT>
+void launch_cluster_bwd_t(swit_engine* e, int shot0, int nb, cudaStream_t st) {
+  cudaLaunchAttribute at[1];
+  const cudaLaunchConfig_t cfg = cluster_config(e->clb, nb, e->maxt, e->smb, st, at);
+  cudaLaunchKernelEx(&cfg, k_bwd_cl<R, MAXT>, make_grid<R>(e), make_rec(e), make_src(e), (const R*)e->src,
+                     (const R*)e->adj_t, (const R*)e->pe, (const R*)e->ue, (const R*)e->we, (R*)e->dg, (R*)e->dfw,
+                     (R*)e->dbk, (const R*)e->strips, shot0);
+}
+
 // Forward time loop of shots [shot0, shot0+nb): fdcore.f90:75-160.
 template <class R>
 void launch_forward_steps(swit_engine* e, bool store, int shot0, int nb, cudaStream_t st) {
+  if (e->variant == 4) {
+    if (e->maxt == 512)
+      launch_cluster_fwd_t<R, 512>(e, store, shot0, nb, st);
+    else
+      launch_cluster_fwd_t<R, 1024>(e, store, shot0, nb, st);
+    return;
+  }
   if (e->variant == 3) {
     Grid<R> g = make_grid<R>(e);
     R* strips = store ? (R*)e->strips : nullptr;
@@ -258,6 +310,13 @@ void launch_forward_steps(swit_engine* e, bool store, int shot0, int nb, cudaStr
 // Reverse time loop of shots [shot0, shot0+nb): solver.f90:230-253.
 template <class R>
 void launch_backward_steps(swit_engine* e, int shot0, int nb, cudaStream_t st) {
+  if (e->variant == 4) {
+    if (e->maxt == 512)
+      launch_cluster_bwd_t<R, 512>(e, shot0, nb, st);
+    else
+      launch_cluster_bwd_t<R, 1024>(e, shot0, nb, st);
+    return;
+  }
   if (e->variant == 3) {
     Grid<R> g = make_grid<R>(e);
     const dim3 grid = vec_grid(e, nb);
@@ -536,8 +595,8 @@ int set_model_impl(swit_engine* e, const float* vp, const float* rho, cudaStream
       damp[i] = kappa * xa * xa;
     }
   }
-  const int LDI = e->variant == 3 ? LD : e->LDI, IL = e->IL;
-  const size_t nci = e->variant == 3 ? (size_t)NX * LD : (size_t)nx * e->LDI;
+  const int LDI = e->variant >= 3 ? LD : e->LDI, IL = e->IL;
+  const size_t nci = e->variant >= 3 ? (size_t)NX * LD : (size_t)nx * e->LDI;
   std::vector<R> A((size_t)NX * LD, R(0)), B((size_t)NX * LD, R(0)), ci(nci, R(1));
   for (int ix = 1; ix <= NX; ++ix)
     for (int iz = 1; iz <= NZ; ++iz) {
@@ -551,6 +610,11 @@ int set_model_impl(swit_engine* e, const float* vp, const float* rho, cudaStream
   CK(cudaMemcpyAsync(e->B, B.data(), B.size() * sizeof(R), cudaMemcpyHostToDevice, st));
   CK(cudaMemcpyAsync(e->damp, damp.data(), damp.size() * sizeof(R), cudaMemcpyHostToDevice, st));
   CK(cudaMemcpyAsync(e->cint, ci.data(), ci.size() * sizeof(R), cudaMemcpyHostToDevice, st));
+  if (e->kp) {
+    Grid<R> g = make_grid<R>(e);
+    k_kappa<R><<<nblocks((size_t)NX * LD), 256, 0, st>>>(g, (R*)e->kp, (R*)e->ku, (R*)e->kw);
+    CK(cudaGetLastError());
+  }
   CK(cudaStreamSynchronize(st));  // host vectors go out of scope
   e->model_set = true;
   e->fwd_ready = false;
@@ -618,6 +682,12 @@ int profile_impl(swit_engine* e, int32_t launches[4], double mean_ms[4], cudaStr
     if (q) CK(cudaMemsetAsync(q, 0, fb, st));
   for (int s0 = 0; s0 < e->ns; s0 += nshot_launch) {
     const int nb = std::min(nshot_launch, e->ns - s0);
+    if (e->variant == 4) {
+      record(0);
+      launch_forward_steps<R>(e, true, s0, nb, st);
+      record(0);
+      continue;
+    }
     dim3 grid, block;
     stencil_shape(e, nb, grid, block);
     for (int it = 2; it <= e->nt; ++it) {
@@ -658,6 +728,12 @@ int profile_impl(swit_engine* e, int32_t launches[4], double mean_ms[4], cudaStr
   copy_end<R>(e, st);
   for (int s0 = 0; s0 < e->ns; s0 += nshot_launch) {
     const int nb = std::min(nshot_launch, e->ns - s0);
+    if (e->variant == 4) {
+      record(2);
+      launch_backward_steps<R>(e, s0, nb, st);
+      record(2);
+      continue;
+    }
     dim3 grid, block;
     stencil_shape(e, nb, grid, block);
     for (int it = e->nt; it >= 2; --it) {
@@ -748,6 +824,72 @@ int import_impl(swit_engine* e, const float* src, const float* boundary, const f
 // Grid index npml + int(x/dx) + 1 in single precision (fdcore.f90:70, 124).
 inline int gidx(int L, float x, float dx) { return L + (int)(x / dx) + 1; }
 
+// Dynamic shared memory of a cluster CTA: nf fields, nab coefficient arrays
+// and the task list (kernels_cluster.cuh).
+inline size_t cluster_smem(const swit_engine* e, int C, int nf, int nab) {
+  return cl_field_elems(e->NX, C, e->LD, nf, nab) * e->esz + cl_list_entries(e->NX, C, e->LD) * sizeof(uint32_t);
+}
+
+template <class R, int MAXT>
+int cluster_attrs(swit_engine* e) {
+  cudaError_t rc = cudaFuncSetAttribute(k_fwd_cl<R, MAXT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)e->smf);
+  if (rc == cudaSuccess) rc = cudaFuncSetAttribute(k_fwd_cl<R, MAXT>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+  if (rc == cudaSuccess)
+    rc = cudaFuncSetAttribute(k_bwd_cl<R, MAXT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)e->smb);
+  if (rc == cudaSuccess) rc = cudaFuncSetAttribute(k_bwd_cl<R, MAXT>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+  if (rc != cudaSuccess) return fail(SWIT_E_CUDA, "cluster kernel attributes: %s", cudaGetErrorString(rc));
+  // the device must be able to hold one cluster of each kernel at a time
+  cudaLaunchAttribute at[1];
+  int nf = 0, nb = 0;
+  cudaLaunchConfig_t cf = cluster_config(e->clf, 1, e->maxt, e->smf, nullptr, at);
+  rc = cudaOccupancyMaxActiveClusters(&nf, k_fwd_cl<R, MAXT>, &cf);
+  if (rc == cudaSuccess) {
+    cudaLaunchConfig_t cb = cluster_config(e->clb, 1, e->maxt, e->smb, nullptr, at);
+    rc = cudaOccupancyMaxActiveClusters(&nb, k_bwd_cl<R, MAXT>, &cb);
+  }
+  if (rc != cudaSuccess) return fail(SWIT_E_CUDA, "cluster occupancy query: %s", cudaGetErrorString(rc));
+  if (nf < 1 || nb < 1)
+    return fail(SWIT_E_LIMIT, "clusters of %d / %d CTAs with %zu / %zu bytes of shared memory do not fit the device",
+                e->clf, e->clb, e->smf, e->smb);
+  return 0;
+}
+
+// Cluster variant geometry.  want = requested cluster size (0: 16); the
+// forward uses it (A and B on chip when they fit too), the reverse loop the
+// smallest size >= want whose six fields fit.  Every CTA needs >= 2 columns.
+template <class R>
+int setup_cluster(swit_engine* e, int want) {
+  int dev = 0, optin = 0;
+  cudaGetDevice(&dev);
+  if (cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess || optin <= 0)
+    return fail(SWIT_E_CUDA, "cannot query the shared memory per block");
+  const int LD4 = e->LD / 4;
+#ifdef SWIT_CLUSTER_THREADS
+  e->maxt = SWIT_CLUSTER_THREADS;
+#else
+  e->maxt = e->prec ? 512 : 1024;  // 64 registers per thread hold the FP32 bodies, FP64 needs 128
+#endif
+  if (LD4 > e->maxt) return fail(SWIT_E_LIMIT, "the cluster kernels need NZ + 2 npml <= %d", 4 * e->maxt);
+  if (want < 0 || want > 16) return fail(SWIT_E_ARG, "block_x of the cluster kernels (cluster size) must be 0..16");
+  int C = want ? want : 16;
+  if (e->NX / C < 2) C = std::max(1, e->NX / 2);
+  if (cluster_smem(e, C, 3, 0) > (size_t)optin)
+    return fail(SWIT_E_LIMIT, "a cluster of %d CTAs cannot hold the forward wavefields (%zu bytes per CTA > %d)", C,
+                cluster_smem(e, C, 3, 0), optin);
+  e->clf = C;
+  e->ab_local = cluster_smem(e, C, 3, 2) <= (size_t)optin ? 1 : 0;
+  e->smf = cluster_smem(e, C, 3, e->ab_local ? 2 : 0);
+  int Cb = C;
+  while (Cb < 16 && e->NX / (Cb + 1) >= 2 && cluster_smem(e, Cb, 6, 0) > (size_t)optin) ++Cb;
+  if (cluster_smem(e, Cb, 6, 0) > (size_t)optin)
+    return fail(SWIT_E_LIMIT, "no cluster of <= 16 CTAs holds the reverse wavefields (%zu bytes per CTA > %d)",
+                cluster_smem(e, Cb, 6, 0), optin);
+  e->clb = Cb;
+  e->smb = cluster_smem(e, Cb, 6, 0);
+  e->bx = C;
+  return e->maxt == 512 ? cluster_attrs<R, 512>(e) : cluster_attrs<R, 1024>(e);
+}
+
 }  // namespace
 
 extern "C" {
@@ -787,9 +929,9 @@ int swit_create(const swit_desc* d, swit_engine** out) {
   e->dt32 = d->dt;
   e->esz = e->prec ? sizeof(double) : sizeof(float);
   e->batch = d->shots_per_batch > 0 ? std::min(d->shots_per_batch, d->ns) : d->ns;
-  if (d->kernel_variant < 0 || d->kernel_variant > 3) {
+  if (d->kernel_variant < 0 || d->kernel_variant > 4) {
     delete e;
-    return fail(SWIT_E_ARG, "kernel_variant must be 0, 1, 2 or 3");
+    return fail(SWIT_E_ARG, "kernel_variant must be 0, 1, 2, 3 or 4");
   }
   e->variant = d->kernel_variant ? d->kernel_variant : 3;
   if (e->variant == 2 && e->LD > 1024) {
@@ -801,6 +943,12 @@ int swit_create(const swit_desc* d, swit_engine** out) {
     if (e->bx != 8 && e->bx != 16 && e->bx != 32) {
       delete e;
       return fail(SWIT_E_ARG, "block_x of the fused kernels must be 8, 16 or 32");
+    }
+  } else if (e->variant == 4) {
+    int rc4 = e->prec ? setup_cluster<double>(e, d->block_x) : setup_cluster<float>(e, d->block_x);
+    if (rc4) {
+      delete e;
+      return rc4;
     }
   } else if (e->variant == 3) {
     // one thread per 4-row vector; blocks of 256 / block_x vectors x block_x columns
@@ -816,7 +964,7 @@ int swit_create(const swit_desc* d, swit_engine** out) {
       return fail(SWIT_E_ARG, "block_x of the split kernels must be a power of two <= 8");
     }
   }
-  e->IL = e->variant == 3 ? e->L : 0;
+  e->IL = e->variant >= 3 ? e->L : 0;
   cudaGetDevice(&e->device);
 
   // geometry: indices exactly as fdcore.f90:70-72, 124-126, 217-218, 349-359
@@ -911,11 +1059,16 @@ int swit_create(const swit_desc* d, swit_engine** out) {
   AL(valloc(e, &e->A, FSZ));
   AL(valloc(e, &e->B, FSZ));
   AL(valloc(e, &e->damp, (size_t)L + 1));
-  AL(valloc(e, &e->cint, e->variant == 3 ? FSZ : FSI));
+  AL(valloc(e, &e->cint, e->variant >= 3 ? FSZ : FSI));
+  if (e->variant >= 3) {
+    AL(valloc(e, &e->kp, FSZ));
+    AL(valloc(e, &e->ku, FSZ));
+    AL(valloc(e, &e->kw, FSZ));
+  }
   void** fields[] = {&e->p, &e->u, &e->w, &e->pb, &e->ub, &e->wb};
   for (void** f : fields) AL(valloc(e, f, (size_t)ns * FSZ));
   void** ifields[] = {&e->pe, &e->ue, &e->we, &e->dg, &e->dfw, &e->dbk};
-  for (void** f : ifields) AL(valloc(e, f, (size_t)ns * (e->variant == 3 ? FSZ : FSI)));
+  for (void** f : ifields) AL(valloc(e, f, (size_t)ns * (e->variant >= 3 ? FSZ : FSI)));
   if (e->variant == 2) {
     void** f2[] = {&e->p2, &e->u2, &e->w2, &e->pb2, &e->ub2, &e->wb2};
     for (void** f : f2) AL(valloc(e, f, (size_t)ns * FSZ));
@@ -961,8 +1114,8 @@ int swit_create(const swit_desc* d, swit_engine** out) {
   const int waves = (ns + e->batch - 1) / e->batch;
   const int per = e->path == 1 ? ns : waves;
   const int per_step = e->variant == 2 ? 1 : 2;
-  e->launches_fwd = per * (e->nt - 1) * per_step;
-  e->launches_bwd = per * (e->nt - 1) * per_step;
+  e->launches_fwd = e->variant == 4 ? per : per * (e->nt - 1) * per_step;
+  e->launches_bwd = e->variant == 4 ? per : per * (e->nt - 1) * per_step;
   *out = e;
   return 0;
 }

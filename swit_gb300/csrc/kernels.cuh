@@ -34,6 +34,10 @@ struct Grid {
   const R* __restrict__ A;     // den c^2 dt / dx   (fdcore.f90:79)
   const R* __restrict__ B;     // dt / (den dx)     (fdcore.f90:99)
   const R* __restrict__ damp;  // damp(1..L) at [1..L]  (pml.f90:84-87)
+  // damping factors per point of the PML-grid layout (k_kappa; vectorised kernels)
+  const R* __restrict__ kp;    // damp(iz,ix) dt
+  const R* __restrict__ ku;    // (damp(iz,ix) + damp(iz,ix+1)) dt / 2
+  const R* __restrict__ kw;    // (damp(iz,ix) + damp(iz+1,ix)) dt / 2
 };
 
 // Receiver tables: per shot a CSR over grid columns 1..NX.  Entries of column ix
@@ -101,6 +105,28 @@ __host__ __device__ inline R damp_at(const R* damp, int iz, int ix, int L, int N
     if (ix >= L - k + 2 && ix <= NX - L + k - 1) v = damp[k];
   }
   return v;
+}
+
+// Damping factors of the pressure and the two velocity updates at every point
+// of the PML grid (LD rows per column), each in the expression and order its
+// update uses (fdcore.f90:80, 100, 109; adjoint 313, 322, 340), so a kernel that
+// loads them computes the same values as one that evaluates damp_at.
+template <class R>
+__global__ void k_kappa(Grid<R> g, R* kp, R* ku, R* kw) {
+  const size_t n = (size_t)g.NX * g.LD;
+  for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x) {
+    const int ix = (int)(t / g.LD) + 1, iz = (int)(t % g.LD) + 1;
+    R a = R(0), b = R(0), c = R(0);
+    if (iz <= g.NZ) {
+      const R d = damp_at(g.damp, iz, ix, g.L, g.NX, g.NZ);
+      a = d * g.dt;
+      if (ix + 1 <= g.NX) b = R(0.5) * (d + damp_at(g.damp, iz, ix + 1, g.L, g.NX, g.NZ)) * g.dt;
+      if (iz + 1 <= g.NZ) c = R(0.5) * (d + damp_at(g.damp, iz + 1, ix, g.L, g.NX, g.NZ)) * g.dt;
+    }
+    kp[t] = a;
+    ku[t] = b;
+    kw[t] = c;
+  }
 }
 
 // ---------------------------------------------------------------------------

@@ -67,12 +67,20 @@ __device__ __forceinline__ void st4_except(R* p, size_t k4, const V4<R>& v, int 
 // reads are mostly the block's own columns (L1 hits).
 struct VecIdx {
   int s, ix, iz0, q;
-  size_t k4;  // vector index within the shot
+  size_t k4;  // vector index of the wavefield arrays (column stride LD/4)
+  size_t kc;  // vector index of the coefficient arrays A, B
+  size_t kg;  // vector index of the per-shot imaging sums dg, dfw, dbk and the kappa arrays
   bool ok;
   bool dint;  // columns ix, ix+1 and rows iz0..iz0+4 all interior: every damping term is 0
   bool deep;  // columns [L+3, NX-L-3], rows [L+4, NZ-L-3]: every update range holds, no
               // strip, mirror or re-insert row or column, no damping
 };
+template <class R>
+__device__ __forceinline__ void vec_flags(const Grid<R>& g, VecIdx& v) {
+  v.dint = v.ix > g.L && v.ix + 1 <= g.NX - g.L && v.iz0 > g.L && v.iz0 + 4 <= g.NZ - g.L;
+  v.deep = v.ix >= g.L + 3 && v.ix <= g.NX - g.L - 3 && v.iz0 >= g.L + 4 && v.iz0 + 3 <= g.NZ - g.L - 3;
+}
+
 template <class R>
 __device__ __forceinline__ VecIdx vec_index(const Grid<R>& g, int shot0) {
   VecIdx v;
@@ -83,13 +91,25 @@ __device__ __forceinline__ VecIdx vec_index(const Grid<R>& g, int shot0) {
   v.ok = v.q < LD4 && v.ix <= g.NX;
   v.iz0 = 4 * v.q + 1;
   v.k4 = (size_t)(v.ix - 1) * LD4 + v.q;
-  v.dint = v.ix > g.L && v.ix + 1 <= g.NX - g.L && v.iz0 > g.L && v.iz0 + 4 <= g.NZ - g.L;
-  v.deep = v.ix >= g.L + 3 && v.ix <= g.NX - g.L - 3 && v.iz0 >= g.L + 4 && v.iz0 + 3 <= g.NZ - g.L - 3;
+  v.kc = v.k4;
+  v.kg = v.k4;
+  vec_flags(g, v);
   return v;
 }
 
-// Damping at (iz, ix) of a vector: 0 on the fast path and for interior vectors.
-#define DAMPV(iz, ix) ((FAST || v.dint) ? R(0) : damp_at(g.damp, (iz), (ix), g.L, g.NX, g.NZ))
+// Damping loads of a body of tier T from the global kappa arrays (indexed like
+// the imaging sums): none on the fast path, where every factor is 0.
+template <class R, int T>
+__device__ __forceinline__ V4<R> kappa4(const R* k, const VecIdx& v) {
+  V4<R> z;
+  if constexpr (T == 0) {
+#pragma unroll
+    for (int j = 0; j < 4; ++j) z.x[j] = R(0);
+  } else {
+    z = ld4(k, v.kg);
+  }
+  return z;
+}
 
 // z-neighbours: the rows iz0+lo .. iz0+4+hi-1 of column ix around vector k4, as an
 // array r[0 .. 4-lo+hi-1] (r[-lo] is row iz0); rows outside the column read 0.
@@ -126,23 +146,25 @@ __device__ __forceinline__ void col_window(const R* f, const VecIdx& v, int LD4,
 
 // ---------------------------------------------------------------------------
 // Forward pressure phase (fdcore.f90:77-94).
-template <class R, bool FAST>
+template <class R, int T>
 __device__ __forceinline__ void fwd_p_body(const Grid<R>& g, const Sources& src, const R* __restrict__ s_fwd, R* __restrict__ p,
                                            const R* __restrict__ u, const R* __restrict__ w, int it,
                                            const VecIdx& v) {
+  constexpr bool CHK = T == 2;
   const int LD4 = g.LD >> 2, ix = v.ix, iz0 = v.iz0, fs = g.fs, NZ = g.NZ;
   V4<R> pv = ld4(p, v.k4);
   bool dirty = false;
-  if (FAST || (ix >= 3 && ix <= g.NX - 2 && iz0 + 3 >= fs + 1 && iz0 <= NZ - 2)) {
-    const V4<R> a = ld4(g.A, v.k4);
+  if (!CHK || (ix >= 3 && ix <= g.NX - 2 && iz0 + 3 >= fs + 1 && iz0 <= NZ - 2)) {
+    const V4<R> a = ld4(g.A, v.kc);
+    const V4<R> kk = kappa4<R, T>(g.kp, v);
     const V4<R> u0 = ld4(u, v.k4), um1 = ld4(u, v.k4 - LD4), up1 = ld4(u, v.k4 + LD4), um2 = ld4(u, v.k4 - 2 * LD4);
     R wz[7];  // w at rows iz0-2 .. iz0+4
     col_window(w, v, LD4, ld4(w, v.k4), wz, -2, 1);
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
       const int iz = iz0 + j;
-      if (FAST || (iz >= fs + 1 && iz <= NZ - 2)) {
-        const R kappa = DAMPV(iz, ix) * g.dt;
+      if (!CHK || (iz >= fs + 1 && iz <= NZ - 2)) {
+        const R kappa = T == 0 ? R(0) : kk.x[j];
         pv.x[j] = (R(1.0) - kappa) * pv.x[j] -
                   a.x[j] * (g.c1 * (u0.x[j] - um1.x[j] + wz[j + 2] - wz[j + 1]) +
                             g.c2 * (up1.x[j] - um2.x[j] + wz[j + 3] - wz[j]));
@@ -150,7 +172,7 @@ __device__ __forceinline__ void fwd_p_body(const Grid<R>& g, const Sources& src,
     }
     dirty = true;
   }
-  if (!FAST) {
+  if (CHK) {
     const int js = src.isz[v.s] - iz0;
     if (ix == src.isx[v.s] && js >= 0 && js < 4) {
       pv.x[js] = pv.x[js] + g.dt * s_fwd[(size_t)v.s * (g.nt + 1) + (it - 1)];
@@ -165,11 +187,79 @@ __device__ __forceinline__ void fwd_p_body(const Grid<R>& g, const Sources& src,
         pv.x[jm] = -pv.x[jp];
         dirty = true;
       } else {
-        p[(size_t)(ix - 1) * g.LD + (fs - 2)] = -pv.x[jp];
+        p[(v.k4 - v.q) * 4 + (fs - 2)] = -pv.x[jp];
       }
     }
   }
   if (dirty) st4(p, v.k4, pv);
+}
+
+// Body tier of a vector in each phase: 0 = fast (deep interior: no damping, no
+// range test, no special row or column), 1 = regular (every row inside the
+// phase's update ranges, damping from the kappa arrays, no mirror, source,
+// receiver, strip or reconstruction work), 2 = general (every test).  Every
+// tier computes the same values; a higher tier only tests more.
+template <class R>
+__device__ __forceinline__ int tier_fwd_p(const Grid<R>& g, const VecIdx& v, bool src_here) {
+  if (src_here) return 2;
+  if (v.deep) return 0;
+  return (v.ix >= 3 && v.ix <= g.NX - 2 && v.iz0 >= g.fs + 2 && v.iz0 + 3 <= g.NZ - 2) ? 1 : 2;
+}
+
+// The vector holds a row or column of the boundary strips (fdcore.f90:130-159).
+template <class R>
+__device__ __forceinline__ bool strip_vec(const Grid<R>& g, const VecIdx& v) {
+  const int fs = g.fs, NZ = g.NZ, NX = g.NX, L = g.L, iz0 = v.iz0, ix = v.ix;
+  return (iz0 <= fs + 2 && iz0 + 3 >= fs) || (iz0 <= NZ - L && iz0 + 3 >= NZ - L - 1) || ix == L + 1 ||
+         ix == L + 2 || ix == NX - L || ix == NX - L - 1;
+}
+
+template <class R>
+__device__ __forceinline__ int tier_fwd_uw(const Grid<R>& g, const VecIdx& v, bool rec_here) {
+  if (rec_here) return 2;
+  if (v.deep) return 0;
+  return (v.ix >= 2 && v.ix <= g.NX - 2 && v.iz0 >= g.fs + 1 && v.iz0 + 3 <= g.NZ - 2 && !strip_vec(g, v)) ? 1 : 2;
+}
+
+// No row of the vector lies on the interior grid (no reconstruction work).
+template <class R>
+__device__ __forceinline__ bool outside_interior(const Grid<R>& g, const VecIdx& v) {
+  const int jx = v.ix - g.L, jz0 = v.iz0 - g.L;
+  return jx < 1 || jx > g.nx || jz0 + 3 < 1 || jz0 > g.nz;
+}
+
+template <class R>
+__device__ __forceinline__ int tier_bwd_uw(const Grid<R>& g, const VecIdx& v) {
+  if (v.deep) return 0;
+  const bool mirror = g.fs_flag == 1 && v.iz0 <= g.fs && v.iz0 + 3 >= g.fs - 1;  // rows fs-1, fs
+  return (v.ix >= 2 && v.ix <= g.NX - 2 && v.iz0 >= 2 && v.iz0 + 3 <= g.NZ - 2 && !mirror && outside_interior(g, v))
+             ? 1
+             : 2;
+}
+
+template <class R>
+__device__ __forceinline__ int tier_bwd_p(const Grid<R>& g, const VecIdx& v, bool rec_here, bool src_here) {
+  if (rec_here || src_here) return 2;
+  if (v.deep) return 0;
+  const bool mirror = v.iz0 <= g.fs + 1 && v.iz0 + 3 >= g.fs - 1;  // rows fs-1, fs+1
+  return (v.ix >= 3 && v.ix <= g.NX - 2 && v.iz0 >= 3 && v.iz0 + 3 <= g.NZ - 2 && !mirror && outside_interior(g, v))
+             ? 1
+             : 2;
+}
+
+// One vector of the pressure phase in the body of its tier.  p, u, w are the
+// shot's arrays.
+template <class R>
+__device__ __forceinline__ void fwd_p_task(const Grid<R>& g, const Sources& src, const R* __restrict__ s_fwd, R* p,
+                                           const R* u, const R* w, int it, const VecIdx& v) {
+  const bool src_here = v.ix == src.isx[v.s] && src.isz[v.s] >= v.iz0 && src.isz[v.s] < v.iz0 + 4;
+  const int t = tier_fwd_p(g, v, src_here);
+  if (t == 0)
+    fwd_p_body<R, 0>(g, src, s_fwd, p, u, w, it, v);
+  else if (t == 1)
+    fwd_p_body<R, 1>(g, src, s_fwd, p, u, w, it, v);
+  else
+    fwd_p_body<R, 2>(g, src, s_fwd, p, u, w, it, v);
 }
 
 template <class R>
@@ -178,31 +268,30 @@ __global__ void __launch_bounds__(256) k_fwd_p_v(Grid<R> g, Sources src, const R
   const VecIdx v = vec_index(g, shot0);
   if (!v.ok) return;
   const size_t off = (size_t)v.s * g.FSZ;
-  const bool src_here = v.ix == src.isx[v.s] && src.isz[v.s] >= v.iz0 && src.isz[v.s] < v.iz0 + 4;
-  if (v.deep && !src_here)
-    fwd_p_body<R, true>(g, src, s_fwd, P + off, U + off, W + off, it, v);
-  else
-    fwd_p_body<R, false>(g, src, s_fwd, P + off, U + off, W + off, it, v);
+  fwd_p_task<R>(g, src, s_fwd, P + off, U + off, W + off, it, v);
 }
 
 // Forward velocity phase (fdcore.f90:97-159).
-template <class R, bool FAST>
+template <class R, int T>
 __device__ __forceinline__ void fwd_uw_body(const Grid<R>& g, const Receivers& rec, const R* __restrict__ p, R* __restrict__ u,
                                             R* __restrict__ w, R* __restrict__ seis_t, R* __restrict__ strips, int it,
                                             const VecIdx& v) {
+  constexpr bool CHK = T == 2;
   const int LD4 = g.LD >> 2, ix = v.ix, iz0 = v.iz0, fs = g.fs, NZ = g.NZ, NX = g.NX, L = g.L;
   const V4<R> p0 = ld4(p, v.k4);
   V4<R> uv = ld4(u, v.k4), wv = ld4(w, v.k4);
   bool du = false, dw = false;
-  if (FAST || (iz0 + 3 >= fs && iz0 <= NZ - 1 && ix >= 2 && ix <= NX - 1)) {
-    const V4<R> b = ld4(g.B, v.k4);
-    if (FAST || ix <= NX - 2) {
+  if (!CHK || (iz0 + 3 >= fs && iz0 <= NZ - 1 && ix >= 2 && ix <= NX - 1)) {
+    const V4<R> b = ld4(g.B, v.kc);
+    const V4<R> kw = kappa4<R, T>(g.kw, v);
+    if (!CHK || ix <= NX - 2) {
+      const V4<R> ku = kappa4<R, T>(g.ku, v);
       const V4<R> pp1 = ld4(p, v.k4 + LD4), pp2 = ld4(p, v.k4 + 2 * LD4), pm1 = ld4(p, v.k4 - LD4);
 #pragma unroll
       for (int j = 0; j < 4; ++j) {
         const int iz = iz0 + j;
-        if (FAST || (iz >= fs && iz <= NZ - 1)) {
-          const R kappa = R(0.5) * (DAMPV(iz, ix) + DAMPV(iz, ix + 1)) * g.dt;
+        if (!CHK || (iz >= fs && iz <= NZ - 1)) {
+          const R kappa = T == 0 ? R(0) : ku.x[j];
           uv.x[j] = (R(1.0) - kappa) * uv.x[j] - b.x[j] * (g.c1 * (pp1.x[j] - p0.x[j]) + g.c2 * (pp2.x[j] - pm1.x[j]));
         }
       }
@@ -213,14 +302,14 @@ __device__ __forceinline__ void fwd_uw_body(const Grid<R>& g, const Receivers& r
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
       const int iz = iz0 + j;
-      if (FAST || (iz >= fs && iz <= NZ - 2)) {
-        const R kappa = R(0.5) * (DAMPV(iz, ix) + DAMPV(iz + 1, ix)) * g.dt;
+      if (!CHK || (iz >= fs && iz <= NZ - 2)) {
+        const R kappa = T == 0 ? R(0) : kw.x[j];
         wv.x[j] = (R(1.0) - kappa) * wv.x[j] - b.x[j] * (g.c1 * (pz[j + 2] - pz[j + 1]) + g.c2 * (pz[j + 3] - pz[j]));
       }
     }
     dw = true;
   }
-  if (!FAST) {
+  if (CHK) {
     // w(fs-1, ix) = w(fs, ix) for every column (fdcore.f90:116-120).  If row
     // fs-1 ends the vector above, that vector (rows < fs) has no u or w update
     // and its owner stores nothing; the owner of row fs writes the mirror.
@@ -230,13 +319,13 @@ __device__ __forceinline__ void fwd_uw_body(const Grid<R>& g, const Receivers& r
         wv.x[jm] = wv.x[jr];
         dw = true;
       } else {
-        w[(size_t)(ix - 1) * g.LD + (fs - 2)] = wv.x[jr];
+        w[(v.k4 - v.q) * 4 + (fs - 2)] = wv.x[jr];
       }
     }
   }
   if (du) st4(u, v.k4, uv);
   if (dw) st4(w, v.k4, wv);
-  if (FAST) return;
+  if (!CHK) return;
   // receivers (fdcore.f90:123-128)
   if (iz0 + 3 >= rec.zlo[v.s] && iz0 <= rec.zhi[v.s]) {
     const int* cp = rec.colptr + (size_t)v.s * (NX + 2);
@@ -290,38 +379,50 @@ __device__ __forceinline__ void fwd_uw_body(const Grid<R>& g, const Receivers& r
 }
 
 template <class R>
+__device__ __forceinline__ void fwd_uw_task(const Grid<R>& g, const Receivers& rec, const R* p, R* u, R* w,
+                                            R* __restrict__ seis_t, R* __restrict__ strips, int it, const VecIdx& v) {
+  const bool rec_here = v.iz0 + 3 >= rec.zlo[v.s] && v.iz0 <= rec.zhi[v.s];
+  const int t = tier_fwd_uw(g, v, rec_here);
+  if (t == 0)
+    fwd_uw_body<R, 0>(g, rec, p, u, w, seis_t, strips, it, v);
+  else if (t == 1)
+    fwd_uw_body<R, 1>(g, rec, p, u, w, seis_t, strips, it, v);
+  else
+    fwd_uw_body<R, 2>(g, rec, p, u, w, seis_t, strips, it, v);
+}
+
+template <class R>
 __global__ void __launch_bounds__(256) k_fwd_uw_v(Grid<R> g, Receivers rec, const R* __restrict__ P, R* U, R* W,
                                                   R* __restrict__ seis_t, R* __restrict__ strips, int it, int shot0) {
   const VecIdx v = vec_index(g, shot0);
   if (!v.ok) return;
   const size_t off = (size_t)v.s * g.FSZ;
-  const bool rec_here = v.iz0 + 3 >= rec.zlo[v.s] && v.iz0 <= rec.zhi[v.s];
-  if (v.deep && !rec_here)
-    fwd_uw_body<R, true>(g, rec, P + off, U + off, W + off, seis_t, strips, it, v);
-  else
-    fwd_uw_body<R, false>(g, rec, P + off, U + off, W + off, seis_t, strips, it, v);
+  fwd_uw_task<R>(g, rec, P + off, U + off, W + off, seis_t, strips, it, v);
 }
 
 // ---------------------------------------------------------------------------
 // Backward velocity phase: adjoint u, w (fdcore.f90:309-333) and the
 // reconstruction u, w with their re-insert (fdcore.f90:220-247).
-template <class R, bool FAST>
+template <class R, int T>
 __device__ __forceinline__ void bwd_uw_body(const Grid<R>& g, const R* __restrict__ pb, R* __restrict__ ub, R* __restrict__ wb,
                                             const R* __restrict__ pe, R* __restrict__ ue, R* __restrict__ we, const R* __restrict__ strips,
                                             int it, const VecIdx& v) {
+  constexpr bool CHK = T == 2;
   const int LD4 = g.LD >> 2, ix = v.ix, iz0 = v.iz0, fs = g.fs, NZ = g.NZ, NX = g.NX, L = g.L;
   // ---- adjoint: u on ix in [2, NX-2], iz in [2, NZ-1]; w on ix in [2, NX-1], iz in [2, NZ-2]
-  if (FAST || (ix >= 2 && ix <= NX - 1 && iz0 <= NZ - 1)) {
-    const V4<R> a = ld4(g.A, v.k4);
+  if (!CHK || (ix >= 2 && ix <= NX - 1 && iz0 <= NZ - 1)) {
+    const V4<R> a = ld4(g.A, v.kc);
     const V4<R> p0 = ld4(pb, v.k4);
-    if (FAST || ix <= NX - 2) {
+    const V4<R> kw = kappa4<R, T>(g.kw, v);
+    if (!CHK || ix <= NX - 2) {
+      const V4<R> ku = kappa4<R, T>(g.ku, v);
       V4<R> uv = ld4(ub, v.k4);
       const V4<R> pp1 = ld4(pb, v.k4 + LD4), pp2 = ld4(pb, v.k4 + 2 * LD4), pm1 = ld4(pb, v.k4 - LD4);
 #pragma unroll
       for (int j = 0; j < 4; ++j) {
         const int iz = iz0 + j;
-        if (FAST || (iz >= 2 && iz <= NZ - 1)) {
-          const R kappa = R(0.5) * (DAMPV(iz, ix) + DAMPV(iz, ix + 1)) * g.dt;
+        if (!CHK || (iz >= 2 && iz <= NZ - 1)) {
+          const R kappa = T == 0 ? R(0) : ku.x[j];
           uv.x[j] = (R(1.0) - kappa) * uv.x[j] - a.x[j] * (g.c1 * (pp1.x[j] - p0.x[j]) + g.c2 * (pp2.x[j] - pm1.x[j]));
         }
       }
@@ -333,19 +434,19 @@ __device__ __forceinline__ void bwd_uw_body(const Grid<R>& g, const R* __restric
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
       const int iz = iz0 + j;
-      if (FAST || (iz >= 2 && iz <= NZ - 2)) {
-        const R kappa = R(0.5) * (DAMPV(iz, ix) + DAMPV(iz + 1, ix)) * g.dt;
+      if (!CHK || (iz >= 2 && iz <= NZ - 2)) {
+        const R kappa = T == 0 ? R(0) : kw.x[j];
         wv.x[j] = (R(1.0) - kappa) * wv.x[j] - a.x[j] * (g.c1 * (pz[j + 2] - pz[j + 1]) + g.c2 * (pz[j + 3] - pz[j]));
       }
     }
-    if (FAST) {
+    if (!CHK) {
       st4(wb, v.k4, wv);
     } else {
       // w(fs-1, ix) = w(fs, ix) for ix in [2, NX-1] (fdcore.f90:329-333).  When
       // row fs-1 ends the vector above, the owner of row fs writes it and that
       // vector's owner stores its other three rows.
       const int jm = fs - 1 - iz0, jr = fs - iz0;
-      if (g.fs_flag == 1 && jr == 0) wb[(size_t)(ix - 1) * g.LD + (fs - 2)] = wv.x[0];
+      if (g.fs_flag == 1 && jr == 0) wb[(v.k4 - v.q) * 4 + (fs - 2)] = wv.x[0];
       if (g.fs_flag == 1 && jm >= 0 && jm < 4) {
         if (jr < 4) {
           wv.x[jm] = wv.x[jr];
@@ -360,31 +461,31 @@ __device__ __forceinline__ void bwd_uw_body(const Grid<R>& g, const R* __restric
   }
   // ---- reconstruction on the interior
   const int jx = ix - L, jz0 = iz0 - L;
-  if (!FAST && (jx < 1 || jx > g.nx || jz0 + 3 < 1 || jz0 > g.nz)) return;
+  if (T == 1 || (CHK && (jx < 1 || jx > g.nx || jz0 + 3 < 1 || jz0 > g.nz))) return;
   const int nx = g.nx, nz = g.nz, fsi = fs - L;
-  const V4<R> bb = ld4(g.B, v.k4);
+  const V4<R> bb = ld4(g.B, v.kc);
   const V4<R> e0 = ld4(pe, v.k4);
   V4<R> uv = ld4(ue, v.k4), wv = ld4(we, v.k4);
-  if (FAST || (jx >= 2 && jx <= nx - 2)) {
+  if (!CHK || (jx >= 2 && jx <= nx - 2)) {
     const V4<R> ep1 = ld4(pe, v.k4 + LD4), ep2 = ld4(pe, v.k4 + 2 * LD4), em1 = ld4(pe, v.k4 - LD4);
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
       const int jz = jz0 + j;
-      if (FAST || (jz >= fsi + 1 && jz <= nz - 1))
+      if (!CHK || (jz >= fsi + 1 && jz <= nz - 1))
         uv.x[j] = uv.x[j] + bb.x[j] * (g.c1 * (ep1.x[j] - e0.x[j]) + g.c2 * (ep2.x[j] - em1.x[j]));
     }
   }
-  if (FAST || (jx >= 2 && jx <= nx - 1)) {
+  if (!CHK || (jx >= 2 && jx <= nx - 1)) {
     R ez[7];  // pe at rows iz0-1 .. iz0+5 (zero outside the interior)
     col_window(pe, v, LD4, e0, ez, -1, 2);
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
       const int jz = jz0 + j;
-      if (FAST || (jz >= fsi + 1 && jz <= nz - 2))
+      if (!CHK || (jz >= fsi + 1 && jz <= nz - 2))
         wv.x[j] = wv.x[j] + bb.x[j] * (g.c1 * (ez[j + 2] - ez[j + 1]) + g.c2 * (ez[j + 3] - ez[j]));
     }
   }
-  if (!FAST) {
+  if (CHK) {
     const R* b = strips + ((size_t)v.s * g.nt + (it - 2)) * g.SL;  // boundary(:, it-1)
     const StripOff o = strip_offsets(nx, nz);
 #pragma unroll
@@ -401,42 +502,53 @@ __device__ __forceinline__ void bwd_uw_body(const Grid<R>& g, const R* __restric
 }
 
 template <class R>
+__device__ __forceinline__ void bwd_uw_task(const Grid<R>& g, const R* pb, R* ub, R* wb, const R* pe, R* ue, R* we,
+                                            const R* __restrict__ strips, int it, const VecIdx& v) {
+  const int t = tier_bwd_uw(g, v);
+  if (t == 0)
+    bwd_uw_body<R, 0>(g, pb, ub, wb, pe, ue, we, strips, it, v);
+  else if (t == 1)
+    bwd_uw_body<R, 1>(g, pb, ub, wb, pe, ue, we, strips, it, v);
+  else
+    bwd_uw_body<R, 2>(g, pb, ub, wb, pe, ue, we, strips, it, v);
+}
+
+template <class R>
 __global__ void __launch_bounds__(256) k_bwd_uw_v(Grid<R> g, const R* __restrict__ PB, R* UB, R* WB,
                                                   const R* __restrict__ PE, R* UE, R* WE,
                                                   const R* __restrict__ strips, int it, int shot0) {
   const VecIdx v = vec_index(g, shot0);
   if (!v.ok) return;
   const size_t off = (size_t)v.s * g.FSZ;
-  if (v.deep)
-    bwd_uw_body<R, true>(g, PB + off, UB + off, WB + off, PE + off, UE + off, WE + off, strips, it, v);
-  else
-    bwd_uw_body<R, false>(g, PB + off, UB + off, WB + off, PE + off, UE + off, WE + off, strips, it, v);
+  bwd_uw_task<R>(g, PB + off, UB + off, WB + off, PE + off, UE + off, WE + off, strips, it, v);
 }
 
 // ---------------------------------------------------------------------------
 // Backward pressure phase: adjoint p + injection + mirror (fdcore.f90:336-373),
 // reconstruction p with source subtraction and re-insert (fdcore.f90:249-287),
 // imaging sums (solver.f90:237-239).
-template <class R, bool FAST>
+template <class R, int T>
 __device__ __forceinline__ void bwd_p_body(const Grid<R>& g, const Receivers& rec, const Sources& src,
                                            const R* __restrict__ s_fwd, const R* __restrict__ adj_t, R* __restrict__ pb,
                                            const R* __restrict__ ub, const R* __restrict__ wb, R* __restrict__ pe,
                                            const R* __restrict__ ue, const R* __restrict__ we, R* __restrict__ dg, R* __restrict__ dfw, R* __restrict__ dbk,
                                            const R* __restrict__ strips, int it, const VecIdx& v) {
+  constexpr bool CHK = T == 2;
   const int LD4 = g.LD >> 2, ix = v.ix, iz0 = v.iz0, fs = g.fs, NZ = g.NZ, NX = g.NX, L = g.L;
   const V4<R> pold = ld4(pb, v.k4);
   V4<R> pv = pold;
   bool dirty = false;
-  if (FAST || (ix >= 3 && ix <= NX - 2 && iz0 + 3 >= 3 && iz0 <= NZ - 2)) {
-    const V4<R> bcoef = ld4(g.B, v.k4);
+  if (!CHK || (ix >= 3 && ix <= NX - 2 && iz0 + 3 >= 3 && iz0 <= NZ - 2)) {
+    const V4<R> bcoef = ld4(g.B, v.kc);
+    const V4<R> kk = kappa4<R, T>(g.kp, v);
     const V4<R> u0 = ld4(ub, v.k4), um1 = ld4(ub, v.k4 - LD4), up1 = ld4(ub, v.k4 + LD4), um2 = ld4(ub, v.k4 - 2 * LD4);
     R wz[7];  // wb at rows iz0-2 .. iz0+4
     col_window(wb, v, LD4, ld4(wb, v.k4), wz, -2, 1);
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
       const int iz = iz0 + j;
-      if (FAST || (iz >= 3 && iz <= NZ - 2)) {
-        const R kappa = DAMPV(iz, ix) * g.dt;
+      if (!CHK || (iz >= 3 && iz <= NZ - 2)) {
+        const R kappa = T == 0 ? R(0) : kk.x[j];
         pv.x[j] = (R(1.0) - kappa) * pv.x[j] -
                   bcoef.x[j] * (g.c1 * (u0.x[j] - um1.x[j] + wz[j + 2] - wz[j + 1]) +
                                 g.c2 * (up1.x[j] - um2.x[j] + wz[j + 3] - wz[j]));
@@ -444,7 +556,7 @@ __device__ __forceinline__ void bwd_p_body(const Grid<R>& g, const Receivers& re
     }
     dirty = true;
   }
-  if (FAST) {
+  if (!CHK) {
     st4(pb, v.k4, pv);
   } else {
     if (iz0 + 3 >= rec.zlo[v.s] && iz0 <= rec.zhi[v.s]) {
@@ -462,7 +574,7 @@ __device__ __forceinline__ void bwd_p_body(const Grid<R>& g, const Receivers& re
     // row fs-1 lies in the vector above, the owner of row fs+1 writes it and
     // that vector's owner stores its other rows.
     const int jm = fs - 1 - iz0, jp = fs + 1 - iz0;
-    if (jp >= 0 && jp < 4 && jm < 0) pb[(size_t)(ix - 1) * g.LD + (fs - 2)] = -pv.x[jp];
+    if (jp >= 0 && jp < 4 && jm < 0) pb[(v.k4 - v.q) * 4 + (fs - 2)] = -pv.x[jp];
     if (jm >= 0 && jm < 4) {
       if (jp < 4) {
         pv.x[jm] = -pv.x[jp];
@@ -477,35 +589,35 @@ __device__ __forceinline__ void bwd_p_body(const Grid<R>& g, const Receivers& re
 
   // ---- reconstruction p, re-insert, imaging on the interior
   const int jx = ix - L, jz0 = iz0 - L;
-  if (!FAST && (jx < 1 || jx > g.nx || jz0 + 3 < 1 || jz0 > g.nz)) return;
+  if (T == 1 || (CHK && (jx < 1 || jx > g.nx || jz0 + 3 < 1 || jz0 > g.nz))) return;
   const int nx = g.nx, nz = g.nz, fsi = fs - L;
   V4<R> ev = ld4(pe, v.k4);
-  if (!FAST) {
+  if (CHK) {
     const int rj = src.risz[v.s] - jz0;
     if (jx == src.risx[v.s] && rj >= 0 && rj < 4) ev.x[rj] = ev.x[rj] - g.dt * s_fwd[(size_t)v.s * (g.nt + 1) + it];
   }
-  if (FAST || (jx >= 3 && jx <= nx - 2)) {
-    const V4<R> a = ld4(g.A, v.k4);
+  if (!CHK || (jx >= 3 && jx <= nx - 2)) {
+    const V4<R> a = ld4(g.A, v.kc);
     const V4<R> u0 = ld4(ue, v.k4), um1 = ld4(ue, v.k4 - LD4), up1 = ld4(ue, v.k4 + LD4), um2 = ld4(ue, v.k4 - 2 * LD4);
     R wz[7];  // we at rows iz0-2 .. iz0+4
     col_window(we, v, LD4, ld4(we, v.k4), wz, -2, 1);
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
       const int jz = jz0 + j;
-      if (FAST || (jz >= fsi + 2 && jz <= nz - 2))
+      if (!CHK || (jz >= fsi + 2 && jz <= nz - 2))
         ev.x[j] = ev.x[j] + a.x[j] * (g.c1 * (u0.x[j] - um1.x[j] + wz[j + 2] - wz[j + 1]) +
                                       g.c2 * (up1.x[j] - um2.x[j] + wz[j + 3] - wz[j]));
     }
   }
-  V4<R> g0 = ld4(dg, v.k4), f0 = ld4(dfw, v.k4), k0 = ld4(dbk, v.k4);
-  const R* b = FAST ? nullptr : strips + ((size_t)v.s * g.nt + (it - 2)) * g.SL;
+  V4<R> g0 = ld4(dg, v.kg), f0 = ld4(dfw, v.kg), k0 = ld4(dbk, v.kg);
+  const R* b = CHK ? strips + ((size_t)v.s * g.nt + (it - 2)) * g.SL : nullptr;
   const StripOff o = strip_offsets(nx, nz);
 #pragma unroll
   for (int j = 0; j < 4; ++j) {
     const int jz = jz0 + j;
-    if (!FAST && (jz < 1 || jz > nz)) continue;
+    if (CHK && (jz < 1 || jz > nz)) continue;
     R pf = ev.x[j];
-    if (!FAST) {
+    if (CHK) {
       if (jz == nz) pf = b[o.B0 + jx - 1];
       if (jz == nz - 1) pf = b[o.B1 + jx - 1];
       if (jx == 1) pf = b[o.S0 + jz - 1];
@@ -522,9 +634,27 @@ __device__ __forceinline__ void bwd_p_body(const Grid<R>& g, const Receivers& re
     k0.x[j] = k0.x[j] + pv.x[j] * pv.x[j];
   }
   st4(pe, v.k4, ev);
-  st4(dg, v.k4, g0);
-  st4(dfw, v.k4, f0);
-  st4(dbk, v.k4, k0);
+  st4(dg, v.kg, g0);
+  st4(dfw, v.kg, f0);
+  st4(dbk, v.kg, k0);
+}
+
+// dg, dfw, dbk are the shot's imaging sums (indexed by v.kg).
+template <class R>
+__device__ __forceinline__ void bwd_p_task(const Grid<R>& g, const Receivers& rec, const Sources& src,
+                                           const R* __restrict__ s_fwd, const R* __restrict__ adj_t, R* pb,
+                                           const R* ub, const R* wb, R* pe, const R* ue, const R* we, R* dg, R* dfw,
+                                           R* dbk, const R* __restrict__ strips, int it, const VecIdx& v) {
+  const bool rec_here = v.iz0 + 3 >= rec.zlo[v.s] && v.iz0 <= rec.zhi[v.s];
+  const int rz = src.risz[v.s] + g.L;  // reconstruction source row on the PML grid (risx = 0: none)
+  const bool src_here = src.risx[v.s] + g.L == v.ix && rz >= v.iz0 && rz < v.iz0 + 4;
+  const int t = tier_bwd_p(g, v, rec_here, src_here);
+  if (t == 0)
+    bwd_p_body<R, 0>(g, rec, src, s_fwd, adj_t, pb, ub, wb, pe, ue, we, dg, dfw, dbk, strips, it, v);
+  else if (t == 1)
+    bwd_p_body<R, 1>(g, rec, src, s_fwd, adj_t, pb, ub, wb, pe, ue, we, dg, dfw, dbk, strips, it, v);
+  else
+    bwd_p_body<R, 2>(g, rec, src, s_fwd, adj_t, pb, ub, wb, pe, ue, we, dg, dfw, dbk, strips, it, v);
 }
 
 template <class R>
@@ -536,15 +666,8 @@ __global__ void __launch_bounds__(256) k_bwd_p_v(Grid<R> g, Receivers rec, Sourc
   const VecIdx v = vec_index(g, shot0);
   if (!v.ok) return;
   const size_t off = (size_t)v.s * g.FSZ;
-  const bool rec_here = v.iz0 + 3 >= rec.zlo[v.s] && v.iz0 <= rec.zhi[v.s];
-  const int rz = src.risz[v.s] + g.L;  // reconstruction source row on the PML grid (risx = 0: none)
-  const bool src_here = src.risx[v.s] + g.L == v.ix && rz >= v.iz0 && rz < v.iz0 + 4;
-  if (v.deep && !rec_here && !src_here)
-    bwd_p_body<R, true>(g, rec, src, s_fwd, adj_t, PB + off, UB + off, WB + off, PE + off, UE + off, WE + off,
-                        DG + off, DFW + off, DBK + off, strips, it, v);
-  else
-    bwd_p_body<R, false>(g, rec, src, s_fwd, adj_t, PB + off, UB + off, WB + off, PE + off, UE + off, WE + off,
-                         DG + off, DFW + off, DBK + off, strips, it, v);
+  bwd_p_task<R>(g, rec, src, s_fwd, adj_t, PB + off, UB + off, WB + off, PE + off, UE + off, WE + off, DG + off,
+                DFW + off, DBK + off, strips, it, v);
 }
 
 }  // namespace swit

@@ -45,9 +45,9 @@ class Engine:
         if path not in ("batched", "plain"):
             raise ValueError("path must be 'batched' or 'plain'")
         self.path = path
-        variants = {"auto": 0, "split": 1, "fused": 2, "vec": 3}
+        variants = {"auto": 0, "split": 1, "fused": 2, "vec": 3, "cluster": 4}
         if kernel not in variants:
-            raise ValueError("kernel must be 'auto', 'split', 'fused' or 'vec'")
+            raise ValueError("kernel must be 'auto', 'split', 'fused', 'vec' or 'cluster'")
         self._keep = dict(
             ng=np.ascontiguousarray(np.full(self.ns, self.ngmax) if ng is None else ng, dtype=np.int32),
             xs=np.ascontiguousarray(src_xz[:, 0]), zs=np.ascontiguousarray(src_xz[:, 1]),
@@ -178,8 +178,11 @@ class Engine:
         ms = (C.c_double * 4)()
         _lib.check(self._lib.swit_profile_kernels(self._h, n, ms, torch.cuda.current_stream().cuda_stream))
         names = ("fwd_p", "fwd_uw", "bwd_uw", "bwd_p")
-        if self.query()["kernel"] == "fused":
+        kind = self.query()["kernel"]
+        if kind == "fused":
             names = ("fwd_step", None, "bwd_step", None)
+        elif kind == "cluster":
+            names = ("fwd_loop", None, "bwd_loop", None)
         return {k: dict(launches=int(n[i]), mean_ms=float(ms[i])) for i, k in enumerate(names) if k}
 
     def query(self):
@@ -188,7 +191,7 @@ class Engine:
         _lib.check(self._lib.swit_query(self._h, C.byref(by), C.byref(sb), C.byref(bx), C.byref(kf), C.byref(kb),
                                         C.byref(kv)))
         return dict(device_bytes=by.value, shots_per_batch=sb.value, block_x=bx.value, kernels_per_forward=kf.value,
-                    kernels_per_backward=kb.value, kernel={1: "split", 2: "fused", 3: "vec"}.get(kv.value, "?"))
+                    kernels_per_backward=kb.value, kernel={1: "split", 2: "fused", 3: "vec", 4: "cluster"}.get(kv.value, "?"))
 
     def close(self):
         if getattr(self, "_h", None):

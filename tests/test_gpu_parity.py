@@ -56,7 +56,7 @@ def test_forward_seismograms_match_oracle(base):
     np.testing.assert_array_equal(seis, base["ref"]["seis"])
 
 
-@pytest.mark.parametrize("kernel", ["split", "vec"])
+@pytest.mark.parametrize("kernel", ["split", "vec", "cluster"])
 def test_boundary_strips_and_end_states_match_oracle(base, kernel):
     s = base["s"]
     with engine(s, kernel=kernel) as e:
@@ -99,7 +99,11 @@ def test_gradient_l2_single_call_matches_oracle(base):
                                   dict(kernel="split", block_x=1), dict(kernel="split", path="plain"),
                                   dict(kernel="split", shots_per_batch=2), dict(kernel="vec"),
                                   dict(kernel="vec", path="plain"), dict(kernel="vec", shots_per_batch=2),
-                                  dict(kernel="vec", block_x=4), dict(kernel="vec", block_x=64)])
+                                  dict(kernel="vec", block_x=4), dict(kernel="vec", block_x=64),
+                                  dict(kernel="cluster"), dict(kernel="cluster", block_x=1),
+                                  dict(kernel="cluster", block_x=2), dict(kernel="cluster", block_x=3),
+                                  dict(kernel="cluster", block_x=7), dict(kernel="cluster", path="plain"),
+                                  dict(kernel="cluster", shots_per_batch=2)])
 def test_launch_variants_are_identical(base, opts):
     s = base["s"]
     with engine(s, **opts) as e:
@@ -111,7 +115,7 @@ def test_launch_variants_are_identical(base, opts):
     np.testing.assert_array_equal(bk, base["grad"]["bk"])
 
 
-@pytest.mark.parametrize("kernel", ["fused", "split", "vec"])
+@pytest.mark.parametrize("kernel", ["fused", "split", "vec", "cluster"])
 def test_fp64_build_matches_fp64_oracle(base, kernel):
     s, pb = base["s"], base["pb"]
     ref = O.forward(pb, s.vp_true, base["rho"], base["src"], store=True, fp64=True)
@@ -136,7 +140,7 @@ def test_repeated_backward_after_one_forward(base):
     np.testing.assert_array_equal(g2, base["grad"]["g"])
 
 
-@pytest.mark.parametrize("kernel", ["fused", "split", "vec"])
+@pytest.mark.parametrize("kernel", ["fused", "split", "vec", "cluster"])
 def test_edge_geometry_surface_receivers_deep_source_uneven_traces(kernel):
     """Receivers on z = 0 (moved one node down), a source deep enough that the
     reconstruction subtracts it (fdcore.f90:250-256), shots with different
@@ -164,7 +168,7 @@ def test_edge_geometry_surface_receivers_deep_source_uneven_traces(kernel):
     np.testing.assert_array_equal(bk, gref["bk"])
 
 
-@pytest.mark.parametrize("kernel", ["fused", "split", "vec"])
+@pytest.mark.parametrize("kernel", ["fused", "split", "vec", "cluster"])
 def test_no_free_surface(kernel):
     s, _ = case(nt=200)
     s.free_surface = 0
@@ -213,8 +217,9 @@ def test_state_and_model_errors(base):
             e.backward(base["adj"])
 
 
+@pytest.mark.parametrize("kernel", ["vec", "cluster"])
 @pytest.mark.parametrize("npml", [8, 9, 10, 11])
-def test_vec_kernels_every_mirror_alignment(npml):
+def test_vec_kernels_every_mirror_alignment(npml, kernel):
     """The vectorised kernels own 4 rows per thread; npml mod 4 decides whether
     the free-surface mirror rows fs-1 and fs / fs+1 share a vector or not."""
     s = survey.small(nx=36, nz=28, npml=npml, nt=160, ns=2, zs=70.0, zr=0.0)
@@ -224,7 +229,7 @@ def test_vec_kernels_every_mirror_alignment(npml):
     ref = O.forward(pb, s.vp_true, rho, src, store=True)
     adj = np.random.default_rng(npml).standard_normal(ref["seis"].shape).astype(np.float32)
     gref = O.adjoint(pb, s.vp_true, rho, src, adj, ref)
-    with engine(s, kernel="vec") as e:
+    with engine(s, kernel=kernel, **({"block_x": 5} if kernel == "cluster" else {})) as e:
         e.set_model(s.vp_true, rho)
         seis = e.forward(src, save_boundary=True)
         g, fw, bk = e.backward(adj)
@@ -234,7 +239,7 @@ def test_vec_kernels_every_mirror_alignment(npml):
     np.testing.assert_array_equal(bk, gref["bk"])
 
 
-@pytest.mark.parametrize("kernel", ["vec", "split", "fused"])
+@pytest.mark.parametrize("kernel", ["vec", "split", "fused", "cluster"])
 def test_import_snapshot_replaces_the_forward_run(base, kernel):
     """The adjoint job from saved files (fd2dmpi/solver.f90:212-228): export the
     strips and end states, load them into a fresh engine, run only the reverse loop."""
@@ -250,3 +255,10 @@ def test_import_snapshot_replaces_the_forward_run(base, kernel):
     np.testing.assert_array_equal(g, base["grad"]["g"])
     np.testing.assert_array_equal(fw, base["grad"]["fw"])
     np.testing.assert_array_equal(bk, base["grad"]["bk"])
+
+
+def test_cluster_variant_rejects_a_grid_that_does_not_fit_on_chip():
+    """3120 x 720 PML-grid columns need more than 16 CTAs' shared memory."""
+    s = survey.small(nx=3000, nz=600, npml=60, nt=10, ns=1)
+    with pytest.raises(SwitError, match="SWIT_E_LIMIT"):
+        Engine(**s.engine_args(), kernel="cluster")
