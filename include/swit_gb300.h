@@ -83,7 +83,9 @@ typedef struct swit_desc {
                                4 = cluster: one launch per time loop, one
                                thread-block cluster per shot holding its
                                wavefields in distributed shared memory
-                               (SWIT_E_LIMIT when they do not fit)              */
+                               (SWIT_E_LIMIT when they do not fit); 5 = hybrid:
+                               cluster forward loop (all shots in one launch),
+                               vec reverse loop (block_x = cluster size)        */
 } swit_desc;
 
 /* Creates an engine and allocates its device workspace on the current device.

@@ -12,6 +12,7 @@
 #include <cstdio>
 #include <cstring>
 #include <string>
+#include <utility>
 #include <vector>
 
 #include "../../include/swit_gb300.h"
@@ -57,9 +58,16 @@ struct swit_engine {
   float dx32, dt32;
   int batch, bx;
   int variant;  // 1 = split, 2 = fused (one kernel per step, ping-pong), 3 = vec (split, 4 rows per thread),
-                // 4 = cluster (one persistent cluster per shot, wavefields in distributed shared memory)
+                // 4 = cluster (one persistent cluster per shot, wavefields in distributed shared memory),
+                // 5 = hybrid (cluster forward, vec reverse loop)
   // cluster variant: cluster sizes, threads per CTA, A and B on chip, dynamic shared memory
-  int clf = 0, clb = 0, maxt = 0, ab_local = 0;
+  int clf = 0, clb = 0, maxt_f = 0, maxt_b = 0, ab_local = 0;
+  int vbx = 32;  // columns per CTA of the vec kernels (block_x for variant 3)
+  bool pdl = false;  // programmatic dependent launch between the vec step kernels (batched path)
+  // task lists of the four vec kernels (fwd_p, fwd_uw, bwd_uw, bwd_p), kernels_vec.cuh
+  uint32_t* d_list = nullptr;
+  size_t list_stride = 0;
+  int list_n0[4] = {0, 0, 0, 0}, list_n1[4] = {0, 0, 0, 0}, list_len[4] = {0, 0, 0, 0};
   size_t smf = 0, smb = 0;
   int IL;       // interior fields: row/column offset into their layout (npml for vec, else 0)
   int device;
@@ -121,7 +129,7 @@ void release(swit_engine* e) {
   void* ptrs[] = {e->d_zlo, e->d_zhi, e->d_ng, e->d_isx, e->d_isz, e->d_risx, e->d_risz, e->d_colptr, e->d_ig, e->d_zr, e->d_live,
                   e->d_mtrace, e->A, e->B, e->damp, e->cint, e->kp, e->ku, e->kw, e->p, e->u, e->w, e->pb, e->ub, e->wb, e->pe,
                   e->ue, e->we, e->dg, e->dfw, e->dbk, e->strips, e->src, e->seis_t, e->adj_t, e->d_in,
-                  e->d_stage, e->p2, e->u2, e->w2, e->pb2, e->ub2, e->wb2, e->pe2, e->ue2, e->we2};
+                  e->d_stage, e->p2, e->u2, e->w2, e->pb2, e->ub2, e->wb2, e->pe2, e->ue2, e->we2, e->d_list};
   for (void* q : ptrs)
     if (q) cudaFree(q);
 }
@@ -226,11 +234,31 @@ void launch_bwd_step(swit_engine* e, int shot0, int nb, int it, cudaStream_t st)
 #undef BWD
 }
 
-// Tiles of (256 / block_x) vectors along z by block_x columns.
-inline dim3 vec_block(const swit_engine* e) { return dim3(256 / e->bx, e->bx); }
-inline dim3 vec_grid(const swit_engine* e, int nb) {
-  const int vz = 256 / e->bx;
-  return dim3((e->LD / 4 + vz - 1) / vz, (e->NX + e->bx - 1) / e->bx, nb);
+// Launch with programmatic stream serialization when pdl is set: the next
+// kernel's blocks may be scheduled during this one's tail and wait on chip
+// (griddepcontrol.wait in pdl_enter) until it has completed.
+template <class... P, class... A>
+void launch_pdl(bool pdl, void (*k)(P...), dim3 grid, dim3 block, cudaStream_t st, A&&... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = st;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = pdl ? 1 : 0;
+  cudaLaunchKernelEx(&cfg, k, std::forward<A>(args)...);
+}
+
+// Vec kernels: 256 threads per block over the kernel's task list k, nb shots.
+inline VecList vec_list(const swit_engine* e, int k) {
+  return VecList{e->d_list + (size_t)k * e->list_stride, e->list_n0[k], e->list_n1[k], e->list_len[k]};
+}
+inline dim3 vec_block(const swit_engine*) { return dim3(256); }
+inline dim3 vec_grid(const swit_engine* e, int k, int nb) {
+  return dim3((unsigned)std::max(1, (e->list_len[k] + 255) / 256), nb);
 }
 
 // Cluster variant: one launch runs the whole time loop of nb shots, one
@@ -254,7 +282,7 @@ inline cudaLaunchConfig_t cluster_config(int C, int nb, int threads, size_t smem
 template <class R, int MAXT>
 void launch_cluster_fwd_t(swit_engine* e, bool store, int shot0, int nb, cudaStream_t st) {
   cudaLaunchAttribute at[1];
-  const cudaLaunchConfig_t cfg = cluster_config(e->clf, nb, e->maxt, e->smf, st, at);
+  const cudaLaunchConfig_t cfg = cluster_config(e->clf, nb, e->maxt_f, e->smf, st, at);
   R* strips = store ? (R*)e->strips : nullptr;
   cudaLaunchKernelEx(&cfg, k_fwd_cl<R, MAXT>, make_grid<R>(e), make_src(e), make_rec(e), (const R*)e->src, (R*)e->p,
                      (R*)e->u, (R*)e->w, (R*)e->seis_t, strips, shot0, e->ab_local);
@@ -263,7 +291,7 @@ void launch_cluster_fwd_t(swit_engine* e, bool store, int shot0, int nb, cudaStr
 template <class R, int MAXT>
 void launch_cluster_bwd_t(swit_engine* e, int shot0, int nb, cudaStream_t st) {
   cudaLaunchAttribute at[1];
-  const cudaLaunchConfig_t cfg = cluster_config(e->clb, nb, e->maxt, e->smb, st, at);
+  const cudaLaunchConfig_t cfg = cluster_config(e->clb, nb, e->maxt_b, e->smb, st, at);
   cudaLaunchKernelEx(&cfg, k_bwd_cl<R, MAXT>, make_grid<R>(e), make_rec(e), make_src(e), (const R*)e->src,
                      (const R*)e->adj_t, (const R*)e->pe, (const R*)e->ue, (const R*)e->we, (R*)e->dg, (R*)e->dfw,
                      (R*)e->dbk, (const R*)e->strips, shot0);
@@ -272,8 +300,8 @@ void launch_cluster_bwd_t(swit_engine* e, int shot0, int nb, cudaStream_t st) {
 // Forward time loop of shots [shot0, shot0+nb): fdcore.f90:75-160.
 template <class R>
 void launch_forward_steps(swit_engine* e, bool store, int shot0, int nb, cudaStream_t st) {
-  if (e->variant == 4) {
-    if (e->maxt == 512)
+  if (e->variant == 4 || e->variant == 5) {
+    if (e->maxt_f == 512)
       launch_cluster_fwd_t<R, 512>(e, store, shot0, nb, st);
     else
       launch_cluster_fwd_t<R, 1024>(e, store, shot0, nb, st);
@@ -282,12 +310,13 @@ void launch_forward_steps(swit_engine* e, bool store, int shot0, int nb, cudaStr
   if (e->variant == 3) {
     Grid<R> g = make_grid<R>(e);
     R* strips = store ? (R*)e->strips : nullptr;
-    const dim3 grid = vec_grid(e, nb);
+    const dim3 block = vec_block(e), g0 = vec_grid(e, 0, nb), g1 = vec_grid(e, 1, nb);
+    const VecList l0 = vec_list(e, 0), l1 = vec_list(e, 1);
     for (int it = 2; it <= e->nt; ++it) {
-      k_fwd_p_v<R><<<grid, vec_block(e), 0, st>>>(g, make_src(e), (const R*)e->src, (R*)e->p, (const R*)e->u, (const R*)e->w,
-                                         it, shot0);
-      k_fwd_uw_v<R><<<grid, vec_block(e), 0, st>>>(g, make_rec(e), (const R*)e->p, (R*)e->u, (R*)e->w, (R*)e->seis_t, strips,
-                                          it, shot0);
+      launch_pdl(e->pdl, k_fwd_p_v<R>, g0, block, st, g, l0, make_src(e), (const R*)e->src, (R*)e->p,
+                 (const R*)e->u, (const R*)e->w, it, shot0);
+      launch_pdl(e->pdl, k_fwd_uw_v<R>, g1, block, st, g, l1, make_rec(e), (const R*)e->p, (R*)e->u, (R*)e->w,
+                 (R*)e->seis_t, strips, it, shot0);
     }
     return;
   }
@@ -311,22 +340,22 @@ void launch_forward_steps(swit_engine* e, bool store, int shot0, int nb, cudaStr
 template <class R>
 void launch_backward_steps(swit_engine* e, int shot0, int nb, cudaStream_t st) {
   if (e->variant == 4) {
-    if (e->maxt == 512)
+    if (e->maxt_b == 512)
       launch_cluster_bwd_t<R, 512>(e, shot0, nb, st);
     else
       launch_cluster_bwd_t<R, 1024>(e, shot0, nb, st);
     return;
   }
-  if (e->variant == 3) {
+  if (e->variant == 3 || e->variant == 5) {
     Grid<R> g = make_grid<R>(e);
-    const dim3 grid = vec_grid(e, nb);
+    const dim3 block = vec_block(e), g2 = vec_grid(e, 2, nb), g3 = vec_grid(e, 3, nb);
+    const VecList l2 = vec_list(e, 2), l3 = vec_list(e, 3);
     for (int it = e->nt; it >= 2; --it) {
-      k_bwd_uw_v<R><<<grid, vec_block(e), 0, st>>>(g, (const R*)e->pb, (R*)e->ub, (R*)e->wb, (const R*)e->pe, (R*)e->ue,
-                                          (R*)e->we, (const R*)e->strips, it, shot0);
-      k_bwd_p_v<R><<<grid, vec_block(e), 0, st>>>(g, make_rec(e), make_src(e), (const R*)e->src, (const R*)e->adj_t,
-                                         (R*)e->pb, (const R*)e->ub, (const R*)e->wb, (R*)e->pe, (const R*)e->ue,
-                                         (const R*)e->we, (R*)e->dg, (R*)e->dfw, (R*)e->dbk, (const R*)e->strips, it,
-                                         shot0);
+      launch_pdl(e->pdl, k_bwd_uw_v<R>, g2, block, st, g, l2, (const R*)e->pb, (R*)e->ub, (R*)e->wb,
+                 (const R*)e->pe, (R*)e->ue, (R*)e->we, (const R*)e->strips, it, shot0);
+      launch_pdl(e->pdl, k_bwd_p_v<R>, g3, block, st, g, l3, make_rec(e), make_src(e), (const R*)e->src,
+                 (const R*)e->adj_t, (R*)e->pb, (const R*)e->ub, (const R*)e->wb, (R*)e->pe, (const R*)e->ue,
+                 (const R*)e->we, (R*)e->dg, (R*)e->dfw, (R*)e->dbk, (const R*)e->strips, it, shot0);
     }
     return;
   }
@@ -347,6 +376,10 @@ void launch_backward_steps(swit_engine* e, int shot0, int nb, cudaStream_t st) {
   }
 }
 
+// Shots per forward launch: the hybrid variant runs every shot in one cluster
+// launch (the hardware schedules the clusters); the others use the batch.
+inline int fwd_batch(const swit_engine* e) { return e->variant == 5 ? e->ns : e->batch; }
+
 template <class R>
 int run_forward_loop(swit_engine* e, bool store, cudaStream_t st) {
   if (e->path == 1) {
@@ -358,7 +391,8 @@ int run_forward_loop(swit_engine* e, bool store, cudaStream_t st) {
   if (!ex) {
     cudaGraph_t graph;
     CK(cudaStreamBeginCapture(e->cap, cudaStreamCaptureModeThreadLocal));
-    for (int s0 = 0; s0 < e->ns; s0 += e->batch) launch_forward_steps<R>(e, store, s0, std::min(e->batch, e->ns - s0), e->cap);
+    const int fb = fwd_batch(e);
+    for (int s0 = 0; s0 < e->ns; s0 += fb) launch_forward_steps<R>(e, store, s0, std::min(fb, e->ns - s0), e->cap);
     cudaError_t rc = cudaStreamEndCapture(e->cap, &graph);
     if (rc != cudaSuccess) return fail(SWIT_E_CUDA, "forward graph capture: %s", cudaGetErrorString(rc));
     rc = cudaGraphInstantiate(&ex, graph, 0);
@@ -680,9 +714,10 @@ int profile_impl(swit_engine* e, int32_t launches[4], double mean_ms[4], cudaStr
   void* fz[] = {e->p, e->u, e->w, e->p2, e->u2, e->w2};
   for (void* q : fz)
     if (q) CK(cudaMemsetAsync(q, 0, fb, st));
-  for (int s0 = 0; s0 < e->ns; s0 += nshot_launch) {
-    const int nb = std::min(nshot_launch, e->ns - s0);
-    if (e->variant == 4) {
+  const int nshot_fwd = e->path == 1 ? 1 : fwd_batch(e);
+  for (int s0 = 0; s0 < e->ns; s0 += nshot_fwd) {
+    const int nb = std::min(nshot_fwd, e->ns - s0);
+    if (e->variant == 4 || e->variant == 5) {
       record(0);
       launch_forward_steps<R>(e, true, s0, nb, st);
       record(0);
@@ -698,14 +733,14 @@ int profile_impl(swit_engine* e, int32_t launches[4], double mean_ms[4], cudaStr
         continue;
       }
       if (e->variant == 3) {
-        const dim3 vg = vec_grid(e, nb);
         record(0);
-        k_fwd_p_v<R><<<vg, vec_block(e), 0, st>>>(g, make_src(e), (const R*)e->src, (R*)e->p, (const R*)e->u, (const R*)e->w,
-                                         it, s0);
+        k_fwd_p_v<R><<<vec_grid(e, 0, nb), vec_block(e), 0, st>>>(g, vec_list(e, 0), make_src(e), (const R*)e->src,
+                                                                (R*)e->p, (const R*)e->u, (const R*)e->w, it, s0);
         record(0);
         record(1);
-        k_fwd_uw_v<R><<<vg, vec_block(e), 0, st>>>(g, make_rec(e), (const R*)e->p, (R*)e->u, (R*)e->w, (R*)e->seis_t,
-                                          (R*)e->strips, it, s0);
+        k_fwd_uw_v<R><<<vec_grid(e, 1, nb), vec_block(e), 0, st>>>(g, vec_list(e, 1), make_rec(e), (const R*)e->p,
+                                                                 (R*)e->u, (R*)e->w, (R*)e->seis_t, (R*)e->strips,
+                                                                 it, s0);
         record(1);
         continue;
       }
@@ -743,17 +778,17 @@ int profile_impl(swit_engine* e, int32_t launches[4], double mean_ms[4], cudaStr
         record(2);
         continue;
       }
-      if (e->variant == 3) {
-        const dim3 vg = vec_grid(e, nb);
+      if (e->variant == 3 || e->variant == 5) {
         record(2);
-        k_bwd_uw_v<R><<<vg, vec_block(e), 0, st>>>(g, (const R*)e->pb, (R*)e->ub, (R*)e->wb, (const R*)e->pe, (R*)e->ue,
-                                          (R*)e->we, (const R*)e->strips, it, s0);
+        k_bwd_uw_v<R><<<vec_grid(e, 2, nb), vec_block(e), 0, st>>>(g, vec_list(e, 2), (const R*)e->pb, (R*)e->ub,
+                                                                 (R*)e->wb, (const R*)e->pe, (R*)e->ue, (R*)e->we,
+                                                                 (const R*)e->strips, it, s0);
         record(2);
         record(3);
-        k_bwd_p_v<R><<<vg, vec_block(e), 0, st>>>(g, make_rec(e), make_src(e), (const R*)e->src, (const R*)e->adj_t,
-                                         (R*)e->pb, (const R*)e->ub, (const R*)e->wb, (R*)e->pe, (const R*)e->ue,
-                                         (const R*)e->we, (R*)e->dg, (R*)e->dfw, (R*)e->dbk, (const R*)e->strips,
-                                         it, s0);
+        k_bwd_p_v<R><<<vec_grid(e, 3, nb), vec_block(e), 0, st>>>(
+            g, vec_list(e, 3), make_rec(e), make_src(e), (const R*)e->src, (const R*)e->adj_t, (R*)e->pb,
+            (const R*)e->ub, (const R*)e->wb, (R*)e->pe, (const R*)e->ue, (const R*)e->we, (R*)e->dg, (R*)e->dfw,
+            (R*)e->dbk, (const R*)e->strips, it, s0);
         record(3);
         continue;
       }
@@ -821,6 +856,45 @@ int import_impl(swit_engine* e, const float* src, const float* boundary, const f
   return 0;
 }
 
+// Task lists of the vec kernels from the body tier of every vector (k_tiers):
+// per kernel the tier groups 0, 1, 2 (no-work vectors dropped), each ordered by
+// tiles of 256/vbx vectors x vbx columns, q fastest, so a warp covers
+// 32 * vbx / 256 columns of 256 / vbx vectors as a 2-D block of the grid would.
+template <class R>
+int build_lists(swit_engine* e) {
+  const int LD4 = e->LD / 4, NX = e->NX;
+  const size_t n = (size_t)NX * LD4;
+  int* d_t = nullptr;
+  CK(cudaMalloc(&d_t, 4 * n * sizeof(int)));
+  k_tiers<R><<<nblocks(n), 256>>>(make_grid<R>(e), make_src(e), make_rec(e), e->ns, d_t);
+  std::vector<int> t(4 * n);
+  cudaError_t ce = cudaMemcpy(t.data(), d_t, 4 * n * sizeof(int), cudaMemcpyDeviceToHost);
+  cudaFree(d_t);
+  if (ce != cudaSuccess) return fail(SWIT_E_CUDA, "task tiers: %s", cudaGetErrorString(ce));
+  const int TX = e->vbx, TQ = 256 / e->vbx;
+  std::vector<uint32_t> L(4 * n);
+  for (int k = 0; k < 4; ++k) {
+    uint32_t* out = &L[k * n];
+    const int* tk = &t[k * n];
+    int m = 0;
+    for (int tier = 0; tier < 3; ++tier) {
+      if (tier == 1) e->list_n0[k] = m;
+      if (tier == 2) e->list_n1[k] = m;
+      for (int x0 = 0; x0 < NX; x0 += TX)
+        for (int q0 = 0; q0 < LD4; q0 += TQ)
+          for (int x = x0; x < std::min(x0 + TX, NX); ++x)
+            for (int q = q0; q < std::min(q0 + TQ, LD4); ++q)
+              if (tk[(size_t)x * LD4 + q] == tier) out[m++] = ((uint32_t)x << 16) | (uint32_t)q;
+    }
+    e->list_len[k] = m;
+  }
+  e->list_stride = n;
+  int rc = dalloc(e, &e->d_list, 4 * n);
+  if (rc) return rc;
+  CK(cudaMemcpy(e->d_list, L.data(), 4 * n * sizeof(uint32_t), cudaMemcpyHostToDevice));
+  return 0;
+}
+
 // Grid index npml + int(x/dx) + 1 in single precision (fdcore.f90:70, 124).
 inline int gidx(int L, float x, float dx) { return L + (int)(x / dx) + 1; }
 
@@ -830,25 +904,27 @@ inline size_t cluster_smem(const swit_engine* e, int C, int nf, int nab) {
   return cl_field_elems(e->NX, C, e->LD, nf, nab) * e->esz + cl_list_entries(e->NX, C, e->LD) * sizeof(uint32_t);
 }
 
+// Attributes and a one-cluster occupancy check of the forward (fwd) and/or the
+// reverse (bwd) cluster kernel with MAXT threads.
 template <class R, int MAXT>
-int cluster_attrs(swit_engine* e) {
-  cudaError_t rc = cudaFuncSetAttribute(k_fwd_cl<R, MAXT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)e->smf);
-  if (rc == cudaSuccess) rc = cudaFuncSetAttribute(k_fwd_cl<R, MAXT>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
-  if (rc == cudaSuccess)
-    rc = cudaFuncSetAttribute(k_bwd_cl<R, MAXT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)e->smb);
-  if (rc == cudaSuccess) rc = cudaFuncSetAttribute(k_bwd_cl<R, MAXT>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
-  if (rc != cudaSuccess) return fail(SWIT_E_CUDA, "cluster kernel attributes: %s", cudaGetErrorString(rc));
-  // the device must be able to hold one cluster of each kernel at a time
+int cluster_attrs(swit_engine* e, bool fwd, bool bwd) {
+  cudaError_t rc = cudaSuccess;
   cudaLaunchAttribute at[1];
-  int nf = 0, nb = 0;
-  cudaLaunchConfig_t cf = cluster_config(e->clf, 1, e->maxt, e->smf, nullptr, at);
-  rc = cudaOccupancyMaxActiveClusters(&nf, k_fwd_cl<R, MAXT>, &cf);
-  if (rc == cudaSuccess) {
-    cudaLaunchConfig_t cb = cluster_config(e->clb, 1, e->maxt, e->smb, nullptr, at);
-    rc = cudaOccupancyMaxActiveClusters(&nb, k_bwd_cl<R, MAXT>, &cb);
+  int n = 1;
+  if (fwd) {
+    rc = cudaFuncSetAttribute(k_fwd_cl<R, MAXT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)e->smf);
+    if (rc == cudaSuccess) rc = cudaFuncSetAttribute(k_fwd_cl<R, MAXT>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+    cudaLaunchConfig_t cf = cluster_config(e->clf, 1, MAXT, e->smf, nullptr, at);
+    if (rc == cudaSuccess) rc = cudaOccupancyMaxActiveClusters(&n, k_fwd_cl<R, MAXT>, &cf);
   }
-  if (rc != cudaSuccess) return fail(SWIT_E_CUDA, "cluster occupancy query: %s", cudaGetErrorString(rc));
-  if (nf < 1 || nb < 1)
+  if (bwd && rc == cudaSuccess && n >= 1) {
+    rc = cudaFuncSetAttribute(k_bwd_cl<R, MAXT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)e->smb);
+    if (rc == cudaSuccess) rc = cudaFuncSetAttribute(k_bwd_cl<R, MAXT>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+    cudaLaunchConfig_t cb = cluster_config(e->clb, 1, MAXT, e->smb, nullptr, at);
+    if (rc == cudaSuccess) rc = cudaOccupancyMaxActiveClusters(&n, k_bwd_cl<R, MAXT>, &cb);
+  }
+  if (rc != cudaSuccess) return fail(SWIT_E_CUDA, "cluster kernel setup: %s", cudaGetErrorString(rc));
+  if (n < 1)
     return fail(SWIT_E_LIMIT, "clusters of %d / %d CTAs with %zu / %zu bytes of shared memory do not fit the device",
                 e->clf, e->clb, e->smf, e->smb);
   return 0;
@@ -864,12 +940,15 @@ int setup_cluster(swit_engine* e, int want) {
   if (cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess || optin <= 0)
     return fail(SWIT_E_CUDA, "cannot query the shared memory per block");
   const int LD4 = e->LD / 4;
-#ifdef SWIT_CLUSTER_THREADS
-  e->maxt = SWIT_CLUSTER_THREADS;
-#else
-  e->maxt = e->prec ? 512 : 1024;  // 64 registers per thread hold the FP32 bodies, FP64 needs 128
+  // 64 registers per thread hold the FP32 bodies, FP64 needs 128
+  e->maxt_f = e->maxt_b = e->prec ? 512 : 1024;
+#ifdef SWIT_CLUSTER_THREADS_F
+  e->maxt_f = SWIT_CLUSTER_THREADS_F;
 #endif
-  if (LD4 > e->maxt) return fail(SWIT_E_LIMIT, "the cluster kernels need NZ + 2 npml <= %d", 4 * e->maxt);
+#ifdef SWIT_CLUSTER_THREADS_B
+  e->maxt_b = SWIT_CLUSTER_THREADS_B;
+#endif
+  if (LD4 > 512) return fail(SWIT_E_LIMIT, "the cluster kernels need NZ + 2 npml <= 2048");
   if (want < 0 || want > 16) return fail(SWIT_E_ARG, "block_x of the cluster kernels (cluster size) must be 0..16");
   int C = want ? want : 16;
   if (e->NX / C < 2) C = std::max(1, e->NX / 2);
@@ -881,13 +960,19 @@ int setup_cluster(swit_engine* e, int want) {
   e->smf = cluster_smem(e, C, 3, e->ab_local ? 2 : 0);
   int Cb = C;
   while (Cb < 16 && e->NX / (Cb + 1) >= 2 && cluster_smem(e, Cb, 6, 0) > (size_t)optin) ++Cb;
-  if (cluster_smem(e, Cb, 6, 0) > (size_t)optin)
-    return fail(SWIT_E_LIMIT, "no cluster of <= 16 CTAs holds the reverse wavefields (%zu bytes per CTA > %d)",
-                cluster_smem(e, Cb, 6, 0), optin);
+  if (cluster_smem(e, Cb, 6, 0) > (size_t)optin) {
+    if (e->variant == 4)
+      return fail(SWIT_E_LIMIT, "no cluster of <= 16 CTAs holds the reverse wavefields (%zu bytes per CTA > %d)",
+                  cluster_smem(e, Cb, 6, 0), optin);
+    Cb = C;  // hybrid: the reverse loop runs the vec kernels; the cluster reverse kernel is never launched
+  }
   e->clb = Cb;
-  e->smb = cluster_smem(e, Cb, 6, 0);
+  e->smb = std::min(cluster_smem(e, Cb, 6, 0), (size_t)optin);
   e->bx = C;
-  return e->maxt == 512 ? cluster_attrs<R, 512>(e) : cluster_attrs<R, 1024>(e);
+  int rc = e->maxt_f == 512 ? cluster_attrs<R, 512>(e, true, false) : cluster_attrs<R, 1024>(e, true, false);
+  if (rc == 0 && e->variant == 4)
+    rc = e->maxt_b == 512 ? cluster_attrs<R, 512>(e, false, true) : cluster_attrs<R, 1024>(e, false, true);
+  return rc;
 }
 
 }  // namespace
@@ -929,9 +1014,9 @@ int swit_create(const swit_desc* d, swit_engine** out) {
   e->dt32 = d->dt;
   e->esz = e->prec ? sizeof(double) : sizeof(float);
   e->batch = d->shots_per_batch > 0 ? std::min(d->shots_per_batch, d->ns) : d->ns;
-  if (d->kernel_variant < 0 || d->kernel_variant > 4) {
+  if (d->kernel_variant < 0 || d->kernel_variant > 5) {
     delete e;
-    return fail(SWIT_E_ARG, "kernel_variant must be 0, 1, 2, 3 or 4");
+    return fail(SWIT_E_ARG, "kernel_variant must be 0..5");
   }
   e->variant = d->kernel_variant ? d->kernel_variant : 3;
   if (e->variant == 2 && e->LD > 1024) {
@@ -944,7 +1029,7 @@ int swit_create(const swit_desc* d, swit_engine** out) {
       delete e;
       return fail(SWIT_E_ARG, "block_x of the fused kernels must be 8, 16 or 32");
     }
-  } else if (e->variant == 4) {
+  } else if (e->variant == 4 || e->variant == 5) {
     int rc4 = e->prec ? setup_cluster<double>(e, d->block_x) : setup_cluster<float>(e, d->block_x);
     if (rc4) {
       delete e;
@@ -952,7 +1037,7 @@ int swit_create(const swit_desc* d, swit_engine** out) {
     }
   } else if (e->variant == 3) {
     // one thread per 4-row vector; blocks of 256 / block_x vectors x block_x columns
-    e->bx = d->block_x > 0 ? d->block_x : 32;
+    e->bx = e->vbx = d->block_x > 0 ? d->block_x : 32;
     if (e->bx != 4 && e->bx != 8 && e->bx != 16 && e->bx != 32 && e->bx != 64) {
       delete e;
       return fail(SWIT_E_ARG, "block_x of the vec kernels must be 4, 8, 16, 32 or 64");
@@ -965,6 +1050,11 @@ int swit_create(const swit_desc* d, swit_engine** out) {
     }
   }
   e->IL = e->variant >= 3 ? e->L : 0;
+#ifdef SWIT_NO_PDL
+  e->pdl = false;
+#else
+  e->pdl = e->path == 0;
+#endif
   cudaGetDevice(&e->device);
 
   // geometry: indices exactly as fdcore.f90:70-72, 124-126, 217-218, 349-359
@@ -1098,6 +1188,14 @@ int swit_create(const swit_desc* d, swit_engine** out) {
     delete e;
     return rc;
   }
+  if (e->variant == 3 || e->variant == 5) {
+    rc = e->prec ? build_lists<double>(e) : build_lists<float>(e);
+    if (rc) {
+      release(e);
+      delete e;
+      return rc;
+    }
+  }
   // Entries never written by the kernels must read as zero: step 1 of the
   // seismograms (fdcore.f90 starts at it = 2), traces beyond ng(is), and the
   // strips of step 1 that the reconstruction inserts at it = 2.
@@ -1114,7 +1212,8 @@ int swit_create(const swit_desc* d, swit_engine** out) {
   const int waves = (ns + e->batch - 1) / e->batch;
   const int per = e->path == 1 ? ns : waves;
   const int per_step = e->variant == 2 ? 1 : 2;
-  e->launches_fwd = e->variant == 4 ? per : per * (e->nt - 1) * per_step;
+  const int fwaves = e->path == 1 ? ns : (ns + fwd_batch(e) - 1) / fwd_batch(e);
+  e->launches_fwd = e->variant >= 4 ? fwaves : per * (e->nt - 1) * per_step;
   e->launches_bwd = e->variant == 4 ? per : per * (e->nt - 1) * per_step;
   *out = e;
   return 0;

@@ -79,43 +79,51 @@ __device__ __forceinline__ void cl_send(cg::cluster_group& cl, R* f, int r, int 
 
 // Task list of a CTA: its vectors (c, q), packed c << 16 | q, grouped by body
 // tier cat(c, q) in {0, 1, 2} (kernels_vec.cuh), each group in column-major
-// order, so a warp runs one body.  n[0] = first vector of tier 1, n[1] = first
-// of tier 2.  Contains __syncthreads; blockDim.x is a multiple of 32 and every
-// thread calls it.
+// order, so 32 consecutive entries run one body; cat 3 = a vector on which the
+// loop does no work, left out.  n[0] = first vector of tier 1, n[1] = first of
+// tier 2, n[2] = length.  Contains __syncthreads; blockDim.x is a multiple of
+// 32 and every thread calls it.
 template <class Cat>
-__device__ __forceinline__ void cl_tasks(uint32_t* list, int ncol, int LD4, Cat cat, int n[2]) {
+__device__ __forceinline__ void cl_tasks(uint32_t* list, int ncol, int LD4, Cat cat, int n[3]) {
   __shared__ int s_cnt[3][32];
   __shared__ int s_off[3];
+  __shared__ int s_len;
   const int tid = threadIdx.x, nthr = blockDim.x, lane = tid & 31, wid = tid >> 5, nw = nthr >> 5;
   const int ntask = ncol * LD4;
-  int c0 = 0, c1 = 0;
+  int c0 = 0, c1 = 0, c2 = 0;
   for (int t = tid; t < ntask; t += nthr) {
     const int k = cat(t / LD4, t % LD4);
     c0 += k == 0;
     c1 += k == 1;
+    c2 += k == 2;
   }
   for (int o = 16; o > 0; o >>= 1) {
     c0 += __shfl_xor_sync(0xffffffffu, c0, o);
     c1 += __shfl_xor_sync(0xffffffffu, c1, o);
+    c2 += __shfl_xor_sync(0xffffffffu, c2, o);
   }
   if (lane == 0) {
     s_cnt[0][wid] = c0;
     s_cnt[1][wid] = c1;
+    s_cnt[2][wid] = c2;
   }
   __syncthreads();
   if (tid == 0) {
-    int a = 0, b = 0;
+    int a = 0, b = 0, c = 0;
     for (int w = 0; w < nw; ++w) {
       a += s_cnt[0][w];
       b += s_cnt[1][w];
+      c += s_cnt[2][w];
     }
     s_off[0] = 0;
     s_off[1] = a;
     s_off[2] = a + b;
+    s_len = a + b + c;
   }
   __syncthreads();
   n[0] = s_off[1];
   n[1] = s_off[2];
+  n[2] = s_len;
   const unsigned lt = (1u << lane) - 1u;
   for (int b = 0; b < ntask; b += nthr) {
     const int t = b + tid;
@@ -141,6 +149,24 @@ __device__ __forceinline__ void cl_tasks(uint32_t* list, int ncol, int LD4, Cat 
       s_off[tid] += a;
     }
     __syncthreads();
+  }
+}
+
+// Dynamic schedule of a phase: warps claim groups of 32 consecutive list
+// entries from an on-chip counter, the last group (general tier) first, so
+// warps that finish early take more work and the strip and trace stores of the
+// general vectors are issued early.  f(i) runs entry i.  The caller resets the
+// counter behind a barrier before the phase runs again.
+template <class F>
+__device__ __forceinline__ void cl_run(int* ctr, int nlist, F f) {
+  const int lane = threadIdx.x & 31, ngrp = (nlist + 31) >> 5;
+  for (;;) {
+    int k = 0;
+    if (lane == 0) k = atomicAdd(ctr, 1);
+    k = __shfl_sync(0xffffffffu, k, 0);
+    if (k >= ngrp) break;
+    const int i = (ngrp - 1 - k) * 32 + lane;
+    if (i < nlist) f(i);
   }
 }
 
@@ -200,7 +226,7 @@ __global__ void __launch_bounds__(MAXT, 1)
     gl.B = b;
   }
   const int isx = src.isx[s], isz = src.isz[s], zlo = rec.zlo[s], zhi = rec.zhi[s];
-  int nt01[2];
+  int nt01[3];
   cl_tasks(list, ncol, LD4, [=](int c, int q) {
     VecIdx v;
     v.ix = x0 + c;
@@ -208,13 +234,17 @@ __global__ void __launch_bounds__(MAXT, 1)
     vec_flags(g, v);
     const bool src_here = v.ix == isx && isz >= v.iz0 && isz < v.iz0 + 4;
     const bool rec_here = v.iz0 + 3 >= zlo && v.iz0 <= zhi;
+    // rows above fs-1 and below NZ-1 take no update, mirror, source, receiver or strip
+    if (v.iz0 + 3 <= g.fs - 1 || v.iz0 >= g.NZ) return 3;
     return max(tier_fwd_p(g, v, src_here), tier_fwd_uw(g, v, rec_here));
   }, nt01);
-  const int n0 = nt01[0], n1 = nt01[1], ntask = ncol * LD4;
+  const int n0 = nt01[0], n1 = nt01[1], nlist = nt01[2];
   const bool abl = ab_local != 0;
+  __shared__ int s_ctr[2];
+  if (tid < 2) s_ctr[tid] = 0;
   cl.sync();
   for (int it = 2; it <= g.nt; ++it) {
-    for (int i = tid; i < ntask; i += nthr) {
+    cl_run(&s_ctr[0], nlist, [&](int i) {
       const uint32_t e = list[i];
       const VecIdx v = cl_index(gl, s, x0, (int)(e >> 16), (int)(e & 0xffffu), abl);
       if (i < n0)
@@ -223,11 +253,12 @@ __global__ void __launch_bounds__(MAXT, 1)
         fwd_p_body<R, 1>(gl, src, s_fwd, p, u, w, it, v);
       else
         fwd_p_body<R, 2>(gl, src, s_fwd, p, u, w, it, v);
-    }
+    });
     __syncthreads();
+    if (tid == 0) s_ctr[0] = 0;
     cl_send(cl, p, r, C, ncol, ncl, LD4);
     cl.sync();
-    for (int i = tid; i < ntask; i += nthr) {
+    cl_run(&s_ctr[1], nlist, [&](int i) {
       const uint32_t e = list[i];
       const VecIdx v = cl_index(gl, s, x0, (int)(e >> 16), (int)(e & 0xffffu), abl);
       if (i < n0)
@@ -236,8 +267,9 @@ __global__ void __launch_bounds__(MAXT, 1)
         fwd_uw_body<R, 1>(gl, rec, p, u, w, seis_t, strips, it, v);
       else
         fwd_uw_body<R, 2>(gl, rec, p, u, w, seis_t, strips, it, v);
-    }
+    });
     __syncthreads();
+    if (tid == 0) s_ctr[1] = 0;
     cl_send(cl, u, r, C, ncol, ncl, LD4);
     cl.sync();
   }
@@ -296,7 +328,7 @@ __global__ void __launch_bounds__(MAXT, 1)
   }
   const int zlo = rec.zlo[s], zhi = rec.zhi[s];
   const int rsx = src.risx[s] + g.L, rsz = src.risz[s] + g.L;  // risx = 0: none
-  int nt01[2];
+  int nt01[3];
   cl_tasks(list, ncol, LD4, [=](int c, int q) {
     VecIdx v;
     v.ix = x0 + c;
@@ -304,15 +336,18 @@ __global__ void __launch_bounds__(MAXT, 1)
     vec_flags(g, v);
     const bool rec_here = v.iz0 + 3 >= zlo && v.iz0 <= zhi;
     const bool src_here = rsx == v.ix && rsz >= v.iz0 && rsz < v.iz0 + 4;
+    if (v.iz0 >= g.NZ) return 3;  // rows below NZ-1 take no update
     return max(tier_bwd_uw(g, v), tier_bwd_p(g, v, rec_here, src_here));
   }, nt01);
-  const int n0 = nt01[0], n1 = nt01[1], ntask = ncol * LD4;
+  const int n0 = nt01[0], n1 = nt01[1], nlist = nt01[2];
+  __shared__ int s_ctr[2];
+  if (tid < 2) s_ctr[tid] = 0;
   cl.sync();
   R* dg = DG + off;
   R* dfw = DFW + off;
   R* dbk = DBK + off;
   for (int it = g.nt; it >= 2; --it) {
-    for (int i = tid; i < ntask; i += nthr) {
+    cl_run(&s_ctr[0], nlist, [&](int i) {
       const uint32_t e = list[i];
       const VecIdx v = cl_index(g, s, x0, (int)(e >> 16), (int)(e & 0xffffu), false);
       if (i < n0)
@@ -321,12 +356,13 @@ __global__ void __launch_bounds__(MAXT, 1)
         bwd_uw_body<R, 1>(g, pb, ub, wb, pe, ue, we, strips, it, v);
       else
         bwd_uw_body<R, 2>(g, pb, ub, wb, pe, ue, we, strips, it, v);
-    }
+    });
     __syncthreads();
+    if (tid == 0) s_ctr[0] = 0;
     cl_send(cl, ub, r, C, ncol, ncl, LD4);
     cl_send(cl, ue, r, C, ncol, ncl, LD4);
     cl.sync();
-    for (int i = tid; i < ntask; i += nthr) {
+    cl_run(&s_ctr[1], nlist, [&](int i) {
       const uint32_t e = list[i];
       const VecIdx v = cl_index(g, s, x0, (int)(e >> 16), (int)(e & 0xffffu), false);
       if (i < n0)
@@ -335,8 +371,9 @@ __global__ void __launch_bounds__(MAXT, 1)
         bwd_p_body<R, 1>(g, rec, src, s_fwd, adj_t, pb, ub, wb, pe, ue, we, dg, dfw, dbk, strips, it, v);
       else
         bwd_p_body<R, 2>(g, rec, src, s_fwd, adj_t, pb, ub, wb, pe, ue, we, dg, dfw, dbk, strips, it, v);
-    }
+    });
     __syncthreads();
+    if (tid == 0) s_ctr[1] = 0;
     cl_send(cl, pb, r, C, ncol, ncl, LD4);
     cl_send(cl, pe, r, C, ncol, ncl, LD4);
     cl.sync();

@@ -62,9 +62,8 @@ __device__ __forceinline__ void st4_except(R* p, size_t k4, const V4<R>& v, int 
     if (j != skip) p[4 * k4 + j] = v.x[j];
 }
 
-// Thread -> (shot, column, first row) of its vector.  A block is a tile of
-// blockDim.x vectors along z by blockDim.y columns, so the x-neighbours a thread
-// reads are mostly the block's own columns (L1 hits).
+// Index set of one vector task: shot, column, first row, and the vector's
+// position in the wavefield, coefficient and imaging-sum arrays.
 struct VecIdx {
   int s, ix, iz0, q;
   size_t k4;  // vector index of the wavefield arrays (column stride LD/4)
@@ -81,20 +80,42 @@ __device__ __forceinline__ void vec_flags(const Grid<R>& g, VecIdx& v) {
   v.deep = v.ix >= g.L + 3 && v.ix <= g.NX - g.L - 3 && v.iz0 >= g.L + 4 && v.iz0 + 3 <= g.NZ - g.L - 3;
 }
 
+// Programmatic dependent launch: wait until the previous kernel in the stream
+// has completed and its writes are visible, then let the next kernel's blocks
+// be scheduled (they wait in the same way).  Without the launch attribute both
+// instructions return at once.
+__device__ __forceinline__ void pdl_enter() {
+  asm volatile("griddepcontrol.wait;\n" ::: "memory");
+  asm volatile("griddepcontrol.launch_dependents;\n" ::: "memory");
+}
+
+
+// Task list of a vectorised kernel: entries (ix - 1) << 16 | q, the vectors
+// grouped by the body tier the kernel needs there (the highest over all
+// shots), each group ordered by 2-D tiles for cache locality; entries [0, n0)
+// run tier 0, [n0, n1) tier 1, [n1, len) tier 2.  Vectors on which the phase
+// does no work are left out.  A warp therefore runs one body.
+struct VecList {
+  const uint32_t* __restrict__ e;
+  int n0, n1, len;
+};
+
+// Thread -> (shot, vector, tier) from the list; false past its end.
 template <class R>
-__device__ __forceinline__ VecIdx vec_index(const Grid<R>& g, int shot0) {
-  VecIdx v;
-  const int LD4 = g.LD >> 2;
-  v.s = shot0 + blockIdx.z;
-  v.q = blockIdx.x * blockDim.x + threadIdx.x;
-  v.ix = blockIdx.y * blockDim.y + threadIdx.y + 1;
-  v.ok = v.q < LD4 && v.ix <= g.NX;
+__device__ __forceinline__ bool list_index(const Grid<R>& g, const VecList& L, int shot0, VecIdx& v, int& t) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= L.len) return false;
+  const uint32_t e = L.e[i];
+  v.s = shot0 + blockIdx.y;
+  v.ix = (int)(e >> 16) + 1;
+  v.q = (int)(e & 0xffffu);
   v.iz0 = 4 * v.q + 1;
-  v.k4 = (size_t)(v.ix - 1) * LD4 + v.q;
+  v.ok = true;
+  v.k4 = (size_t)(v.ix - 1) * (g.LD >> 2) + v.q;
   v.kc = v.k4;
   v.kg = v.k4;
-  vec_flags(g, v);
-  return v;
+  t = i < L.n0 ? 0 : (i < L.n1 ? 1 : 2);
+  return true;
 }
 
 // Damping loads of a body of tier T from the global kappa arrays (indexed like
@@ -247,28 +268,27 @@ __device__ __forceinline__ int tier_bwd_p(const Grid<R>& g, const VecIdx& v, boo
              : 2;
 }
 
-// One vector of the pressure phase in the body of its tier.  p, u, w are the
-// shot's arrays.
-template <class R>
-__device__ __forceinline__ void fwd_p_task(const Grid<R>& g, const Sources& src, const R* __restrict__ s_fwd, R* p,
-                                           const R* u, const R* w, int it, const VecIdx& v) {
-  const bool src_here = v.ix == src.isx[v.s] && src.isz[v.s] >= v.iz0 && src.isz[v.s] < v.iz0 + 4;
-  const int t = tier_fwd_p(g, v, src_here);
-  if (t == 0)
-    fwd_p_body<R, 0>(g, src, s_fwd, p, u, w, it, v);
-  else if (t == 1)
-    fwd_p_body<R, 1>(g, src, s_fwd, p, u, w, it, v);
-  else
-    fwd_p_body<R, 2>(g, src, s_fwd, p, u, w, it, v);
-}
+// Body of tier t (0, 1, 2) of a list entry.
+#define SWIT_TIER_CALL(body, ...) \
+  do {                            \
+    if (t == 0)                   \
+      body<R, 0>(__VA_ARGS__);    \
+    else if (t == 1)              \
+      body<R, 1>(__VA_ARGS__);    \
+    else                          \
+      body<R, 2>(__VA_ARGS__);    \
+  } while (0)
 
 template <class R>
-__global__ void __launch_bounds__(256) k_fwd_p_v(Grid<R> g, Sources src, const R* __restrict__ s_fwd, R* P,
+__global__ void __launch_bounds__(256) k_fwd_p_v(Grid<R> g, VecList L, Sources src, const R* __restrict__ s_fwd, R* P,
                                                  const R* __restrict__ U, const R* __restrict__ W, int it, int shot0) {
-  const VecIdx v = vec_index(g, shot0);
-  if (!v.ok) return;
+  VecIdx v;
+  int t;
+  const bool ok = list_index(g, L, shot0, v, t);
+  pdl_enter();
+  if (!ok) return;
   const size_t off = (size_t)v.s * g.FSZ;
-  fwd_p_task<R>(g, src, s_fwd, P + off, U + off, W + off, it, v);
+  SWIT_TIER_CALL(fwd_p_body, g, src, s_fwd, P + off, U + off, W + off, it, v);
 }
 
 // Forward velocity phase (fdcore.f90:97-159).
@@ -379,25 +399,16 @@ __device__ __forceinline__ void fwd_uw_body(const Grid<R>& g, const Receivers& r
 }
 
 template <class R>
-__device__ __forceinline__ void fwd_uw_task(const Grid<R>& g, const Receivers& rec, const R* p, R* u, R* w,
-                                            R* __restrict__ seis_t, R* __restrict__ strips, int it, const VecIdx& v) {
-  const bool rec_here = v.iz0 + 3 >= rec.zlo[v.s] && v.iz0 <= rec.zhi[v.s];
-  const int t = tier_fwd_uw(g, v, rec_here);
-  if (t == 0)
-    fwd_uw_body<R, 0>(g, rec, p, u, w, seis_t, strips, it, v);
-  else if (t == 1)
-    fwd_uw_body<R, 1>(g, rec, p, u, w, seis_t, strips, it, v);
-  else
-    fwd_uw_body<R, 2>(g, rec, p, u, w, seis_t, strips, it, v);
-}
-
-template <class R>
-__global__ void __launch_bounds__(256) k_fwd_uw_v(Grid<R> g, Receivers rec, const R* __restrict__ P, R* U, R* W,
-                                                  R* __restrict__ seis_t, R* __restrict__ strips, int it, int shot0) {
-  const VecIdx v = vec_index(g, shot0);
-  if (!v.ok) return;
+__global__ void __launch_bounds__(256) k_fwd_uw_v(Grid<R> g, VecList L, Receivers rec, const R* __restrict__ P, R* U,
+                                                  R* W, R* __restrict__ seis_t, R* __restrict__ strips, int it,
+                                                  int shot0) {
+  VecIdx v;
+  int t;
+  const bool ok = list_index(g, L, shot0, v, t);
+  pdl_enter();
+  if (!ok) return;
   const size_t off = (size_t)v.s * g.FSZ;
-  fwd_uw_task<R>(g, rec, P + off, U + off, W + off, seis_t, strips, it, v);
+  SWIT_TIER_CALL(fwd_uw_body, g, rec, P + off, U + off, W + off, seis_t, strips, it, v);
 }
 
 // ---------------------------------------------------------------------------
@@ -502,25 +513,16 @@ __device__ __forceinline__ void bwd_uw_body(const Grid<R>& g, const R* __restric
 }
 
 template <class R>
-__device__ __forceinline__ void bwd_uw_task(const Grid<R>& g, const R* pb, R* ub, R* wb, const R* pe, R* ue, R* we,
-                                            const R* __restrict__ strips, int it, const VecIdx& v) {
-  const int t = tier_bwd_uw(g, v);
-  if (t == 0)
-    bwd_uw_body<R, 0>(g, pb, ub, wb, pe, ue, we, strips, it, v);
-  else if (t == 1)
-    bwd_uw_body<R, 1>(g, pb, ub, wb, pe, ue, we, strips, it, v);
-  else
-    bwd_uw_body<R, 2>(g, pb, ub, wb, pe, ue, we, strips, it, v);
-}
-
-template <class R>
-__global__ void __launch_bounds__(256) k_bwd_uw_v(Grid<R> g, const R* __restrict__ PB, R* UB, R* WB,
+__global__ void __launch_bounds__(256) k_bwd_uw_v(Grid<R> g, VecList L, const R* __restrict__ PB, R* UB, R* WB,
                                                   const R* __restrict__ PE, R* UE, R* WE,
                                                   const R* __restrict__ strips, int it, int shot0) {
-  const VecIdx v = vec_index(g, shot0);
-  if (!v.ok) return;
+  VecIdx v;
+  int t;
+  const bool ok = list_index(g, L, shot0, v, t);
+  pdl_enter();
+  if (!ok) return;
   const size_t off = (size_t)v.s * g.FSZ;
-  bwd_uw_task<R>(g, PB + off, UB + off, WB + off, PE + off, UE + off, WE + off, strips, it, v);
+  SWIT_TIER_CALL(bwd_uw_body, g, PB + off, UB + off, WB + off, PE + off, UE + off, WE + off, strips, it, v);
 }
 
 // ---------------------------------------------------------------------------
@@ -641,33 +643,52 @@ __device__ __forceinline__ void bwd_p_body(const Grid<R>& g, const Receivers& re
 
 // dg, dfw, dbk are the shot's imaging sums (indexed by v.kg).
 template <class R>
-__device__ __forceinline__ void bwd_p_task(const Grid<R>& g, const Receivers& rec, const Sources& src,
-                                           const R* __restrict__ s_fwd, const R* __restrict__ adj_t, R* pb,
-                                           const R* ub, const R* wb, R* pe, const R* ue, const R* we, R* dg, R* dfw,
-                                           R* dbk, const R* __restrict__ strips, int it, const VecIdx& v) {
-  const bool rec_here = v.iz0 + 3 >= rec.zlo[v.s] && v.iz0 <= rec.zhi[v.s];
-  const int rz = src.risz[v.s] + g.L;  // reconstruction source row on the PML grid (risx = 0: none)
-  const bool src_here = src.risx[v.s] + g.L == v.ix && rz >= v.iz0 && rz < v.iz0 + 4;
-  const int t = tier_bwd_p(g, v, rec_here, src_here);
-  if (t == 0)
-    bwd_p_body<R, 0>(g, rec, src, s_fwd, adj_t, pb, ub, wb, pe, ue, we, dg, dfw, dbk, strips, it, v);
-  else if (t == 1)
-    bwd_p_body<R, 1>(g, rec, src, s_fwd, adj_t, pb, ub, wb, pe, ue, we, dg, dfw, dbk, strips, it, v);
-  else
-    bwd_p_body<R, 2>(g, rec, src, s_fwd, adj_t, pb, ub, wb, pe, ue, we, dg, dfw, dbk, strips, it, v);
+__global__ void __launch_bounds__(256) k_bwd_p_v(Grid<R> g, VecList L, Receivers rec, Sources src,
+                                                 const R* __restrict__ s_fwd, const R* __restrict__ adj_t, R* PB,
+                                                 const R* __restrict__ UB, const R* __restrict__ WB, R* PE,
+                                                 const R* __restrict__ UE, const R* __restrict__ WE, R* DG, R* DFW,
+                                                 R* DBK, const R* __restrict__ strips, int it, int shot0) {
+  VecIdx v;
+  int t;
+  const bool ok = list_index(g, L, shot0, v, t);
+  pdl_enter();
+  if (!ok) return;
+  const size_t off = (size_t)v.s * g.FSZ;
+  SWIT_TIER_CALL(bwd_p_body, g, rec, src, s_fwd, adj_t, PB + off, UB + off, WB + off, PE + off, UE + off, WE + off,
+                 DG + off, DFW + off, DBK + off, strips, it, v);
 }
 
+// Body tier of every vector for each phase kernel (fwd_p, fwd_uw, bwd_uw,
+// bwd_p), the highest any shot needs; 3 where the phase does no work: rows
+// above fs-1 in the forward (no update, mirror, source, receiver or strip
+// there) and rows from NZ on.  out[k * NX * LD/4 + (ix-1) * LD/4 + q].
 template <class R>
-__global__ void __launch_bounds__(256) k_bwd_p_v(Grid<R> g, Receivers rec, Sources src, const R* __restrict__ s_fwd,
-                                                 const R* __restrict__ adj_t, R* PB, const R* __restrict__ UB,
-                                                 const R* __restrict__ WB, R* PE, const R* __restrict__ UE,
-                                                 const R* __restrict__ WE, R* DG, R* DFW, R* DBK,
-                                                 const R* __restrict__ strips, int it, int shot0) {
-  const VecIdx v = vec_index(g, shot0);
-  if (!v.ok) return;
-  const size_t off = (size_t)v.s * g.FSZ;
-  bwd_p_task<R>(g, rec, src, s_fwd, adj_t, PB + off, UB + off, WB + off, PE + off, UE + off, WE + off, DG + off,
-                DFW + off, DBK + off, strips, it, v);
+__global__ void k_tiers(Grid<R> g, Sources src, Receivers rec, int ns, int* out) {
+  const int LD4 = g.LD >> 2;
+  const size_t n = (size_t)g.NX * LD4;
+  for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x) {
+    VecIdx v;
+    v.ix = (int)(t / LD4) + 1;
+    v.q = (int)(t % LD4);
+    v.iz0 = 4 * v.q + 1;
+    vec_flags(g, v);
+    int a = 0, b = 0, c = 0, d = 0;
+    for (int s = 0; s < ns; ++s) {
+      const bool fsrc = v.ix == src.isx[s] && src.isz[s] >= v.iz0 && src.isz[s] < v.iz0 + 4;
+      const bool rh = v.iz0 + 3 >= rec.zlo[s] && v.iz0 <= rec.zhi[s];
+      const int rz = src.risz[s] + g.L;
+      const bool bsrc = src.risx[s] + g.L == v.ix && rz >= v.iz0 && rz < v.iz0 + 4;
+      a = max(a, tier_fwd_p(g, v, fsrc));
+      b = max(b, tier_fwd_uw(g, v, rh));
+      c = max(c, tier_bwd_uw(g, v));
+      d = max(d, tier_bwd_p(g, v, rh, bsrc));
+    }
+    const bool fskip = v.iz0 + 3 <= g.fs - 1 || v.iz0 >= g.NZ, bskip = v.iz0 >= g.NZ;
+    out[t] = fskip ? 3 : a;
+    out[n + t] = fskip ? 3 : b;
+    out[2 * n + t] = bskip ? 3 : c;
+    out[3 * n + t] = bskip ? 3 : d;
+  }
 }
 
 }  // namespace swit

@@ -45,9 +45,9 @@ class Engine:
         if path not in ("batched", "plain"):
             raise ValueError("path must be 'batched' or 'plain'")
         self.path = path
-        variants = {"auto": 0, "split": 1, "fused": 2, "vec": 3, "cluster": 4}
+        variants = {"auto": 0, "split": 1, "fused": 2, "vec": 3, "cluster": 4, "hybrid": 5}
         if kernel not in variants:
-            raise ValueError("kernel must be 'auto', 'split', 'fused', 'vec' or 'cluster'")
+            raise ValueError("kernel must be one of %s" % ", ".join(sorted(variants)))
         self._keep = dict(
             ng=np.ascontiguousarray(np.full(self.ns, self.ngmax) if ng is None else ng, dtype=np.int32),
             xs=np.ascontiguousarray(src_xz[:, 0]), zs=np.ascontiguousarray(src_xz[:, 1]),
@@ -183,6 +183,8 @@ class Engine:
             names = ("fwd_step", None, "bwd_step", None)
         elif kind == "cluster":
             names = ("fwd_loop", None, "bwd_loop", None)
+        elif kind == "hybrid":
+            names = ("fwd_loop", None, "bwd_uw", "bwd_p")
         return {k: dict(launches=int(n[i]), mean_ms=float(ms[i])) for i, k in enumerate(names) if k}
 
     def query(self):
@@ -191,7 +193,7 @@ class Engine:
         _lib.check(self._lib.swit_query(self._h, C.byref(by), C.byref(sb), C.byref(bx), C.byref(kf), C.byref(kb),
                                         C.byref(kv)))
         return dict(device_bytes=by.value, shots_per_batch=sb.value, block_x=bx.value, kernels_per_forward=kf.value,
-                    kernels_per_backward=kb.value, kernel={1: "split", 2: "fused", 3: "vec", 4: "cluster"}.get(kv.value, "?"))
+                    kernels_per_backward=kb.value, kernel={1: "split", 2: "fused", 3: "vec", 4: "cluster", 5: "hybrid"}.get(kv.value, "?"))
 
     def close(self):
         if getattr(self, "_h", None):

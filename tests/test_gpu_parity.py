@@ -103,7 +103,9 @@ def test_gradient_l2_single_call_matches_oracle(base):
                                   dict(kernel="cluster"), dict(kernel="cluster", block_x=1),
                                   dict(kernel="cluster", block_x=2), dict(kernel="cluster", block_x=3),
                                   dict(kernel="cluster", block_x=7), dict(kernel="cluster", path="plain"),
-                                  dict(kernel="cluster", shots_per_batch=2)])
+                                  dict(kernel="cluster", shots_per_batch=2), dict(kernel="hybrid"),
+                                  dict(kernel="hybrid", block_x=3, shots_per_batch=2),
+                                  dict(kernel="hybrid", path="plain")])
 def test_launch_variants_are_identical(base, opts):
     s = base["s"]
     with engine(s, **opts) as e:
