@@ -71,8 +71,10 @@ typedef struct swit_desc {
   int32_t shots_per_batch;  /* batched path: shots per launch, 0 = automatic    */
   int32_t block_x;          /* columns per CTA, 0 = automatic: split kernels
                                1, 2, 4 or 8 (x 32 rows); fused kernels 8, 16
-                               or 32 (x all rows); vec kernels 4..64 columns x
-                               256/block_x four-row vectors (default 32);
+                               or 32 (x all rows); vec kernels: task lists
+                               ordered by tiles of block_x columns (a power of
+                               two <= 64, default 4) x 256/block_x four-row
+                               vectors;
                                cluster kernels: CTAs per cluster 1..16 (default
                                16; the reverse loop takes more CTAs when its six
                                wavefields need them)                            */

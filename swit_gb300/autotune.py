@@ -26,12 +26,12 @@ def candidates(ns, nz_pml):
         for tx in (8, 16, 32):
             for b in batches:
                 out.append(dict(kernel="fused", block_x=tx, shots_per_batch=b))
-    for bx in (8, 16, 32):
-        for b in batches:
+    for bx in (1, 2, 4, 8):
+        for b in batches[:2]:
             out.append(dict(kernel="vec", block_x=bx, shots_per_batch=b))
     out.append(dict(kernel="split", block_x=4, shots_per_batch=ns))
-    for cl in (16, 8):
-        out.append(dict(kernel="cluster", block_x=cl, shots_per_batch=ns))
+    out.append(dict(kernel="cluster", block_x=8, shots_per_batch=ns))
+    out.append(dict(kernel="hybrid", block_x=8, shots_per_batch=max(1, (ns + 1) // 2)))
     return out
 
 

@@ -1036,11 +1036,11 @@ int swit_create(const swit_desc* d, swit_engine** out) {
       return rc4;
     }
   } else if (e->variant == 3) {
-    // one thread per 4-row vector; blocks of 256 / block_x vectors x block_x columns
-    e->bx = e->vbx = d->block_x > 0 ? d->block_x : 32;
-    if (e->bx != 4 && e->bx != 8 && e->bx != 16 && e->bx != 32 && e->bx != 64) {
+    // one thread per 4-row vector; task lists ordered by tiles of 256 / block_x vectors x block_x columns
+    e->bx = e->vbx = d->block_x > 0 ? d->block_x : 4;
+    if (e->bx > 64 || (e->bx & (e->bx - 1))) {
       delete e;
-      return fail(SWIT_E_ARG, "block_x of the vec kernels must be 4, 8, 16, 32 or 64");
+      return fail(SWIT_E_ARG, "block_x of the vec kernels must be a power of two <= 64");
     }
   } else {
     e->bx = d->block_x > 0 ? d->block_x : 4;

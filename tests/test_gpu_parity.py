@@ -99,7 +99,8 @@ def test_gradient_l2_single_call_matches_oracle(base):
                                   dict(kernel="split", block_x=1), dict(kernel="split", path="plain"),
                                   dict(kernel="split", shots_per_batch=2), dict(kernel="vec"),
                                   dict(kernel="vec", path="plain"), dict(kernel="vec", shots_per_batch=2),
-                                  dict(kernel="vec", block_x=4), dict(kernel="vec", block_x=64),
+                                  dict(kernel="vec", block_x=1), dict(kernel="vec", block_x=2),
+                                  dict(kernel="vec", block_x=32), dict(kernel="vec", block_x=64),
                                   dict(kernel="cluster"), dict(kernel="cluster", block_x=1),
                                   dict(kernel="cluster", block_x=2), dict(kernel="cluster", block_x=3),
                                   dict(kernel="cluster", block_x=7), dict(kernel="cluster", path="plain"),
