@@ -43,7 +43,7 @@ def parse():
     ap.add_argument("--nt", type=int, default=None, help="time steps (default 4000)")
     ap.add_argument("--batch", type=int, default=0, help="shots per launch (0 = engine default)")
     ap.add_argument("--block-x", type=int, default=0)
-    ap.add_argument("--kernel", default="auto", choices=["auto", "fused", "split", "vec", "cluster", "hybrid"])
+    ap.add_argument("--kernel", default="auto", choices=["auto", "fused", "split", "vec", "cluster", "hybrid", "band"])
     ap.add_argument("--no-tune", action="store_true", help="skip the launch-configuration autotuner")
     ap.add_argument("--no-extras", action="store_true", help="skip plain path, CPU baseline and kernel profile")
     return ap.parse_args()

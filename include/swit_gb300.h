@@ -47,6 +47,7 @@ extern "C" {
 #define SWIT_E_CUDA -6     /* CUDA runtime error                                 */
 #define SWIT_E_NOMEM -7    /* device allocation failed                           */
 #define SWIT_E_LIMIT -8    /* problem larger than a fixed capacity               */
+#define SWIT_E_TIMEOUT -9  /* a kernel stopped waiting on an in-kernel copy      */
 
 typedef struct swit_engine swit_engine;
 
@@ -87,7 +88,10 @@ typedef struct swit_desc {
                                wavefields in distributed shared memory
                                (SWIT_E_LIMIT when they do not fit); 5 = hybrid:
                                cluster forward loop (all shots in one launch),
-                               vec reverse loop (block_x = cluster size)        */
+                               vec reverse loop (block_x = cluster size);
+                               6 = band: the vec bodies on bands of block_x
+                               columns (0 = as many as 256 threads cover) staged
+                               through shared memory by bulk copies            */
 } swit_desc;
 
 /* Creates an engine and allocates its device workspace on the current device.
@@ -190,6 +194,13 @@ int swit_forward_shot_static(int32_t nx, int32_t nz, int32_t npml, int32_t nt, f
 /* Sizes the engine has allocated; any pointer may be NULL. */
 int swit_query(const swit_engine* e, int64_t* device_bytes, int32_t* shots_per_batch, int32_t* block_x,
                int32_t* kernels_per_forward, int32_t* kernels_per_backward, int32_t* kernel_variant);
+
+/* Waits for `stream` and reports whether any kernel of the engine gave up
+ * waiting for the copies it stages into shared memory (band variant: every such
+ * wait is bounded, and a block that times out skips its update).  Returns
+ * SWIT_E_TIMEOUT once for such an event, then clears it.  No counterpart in the
+ * reference, whose CPU loops have no asynchronous copies. */
+int swit_check(swit_engine* e, void* stream);
 
 /* Releases the engine and its device memory. */
 int swit_destroy(swit_engine* e);

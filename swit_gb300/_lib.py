@@ -11,12 +11,12 @@ LIB_PATH = os.path.join(_HERE, "libswit_gb300.so")
 
 SWIT_OK = 0
 ERRORS = {-1: "SWIT_E_ARG", -2: "SWIT_E_GEOM", -3: "SWIT_E_CFL", -4: "SWIT_E_MODEL", -5: "SWIT_E_STATE",
-          -6: "SWIT_E_CUDA", -7: "SWIT_E_NOMEM", -8: "SWIT_E_LIMIT"}
+          -6: "SWIT_E_CUDA", -7: "SWIT_E_NOMEM", -8: "SWIT_E_LIMIT", -9: "SWIT_E_TIMEOUT"}
 
 # every symbol include/swit_gb300.h declares
 EXPORTS = ("swit_create", "swit_set_model", "swit_forward", "swit_backward", "swit_gradient_l2",
            "swit_export_snapshot", "swit_import_snapshot", "swit_profile_kernels", "swit_query", "swit_destroy", "swit_last_error", "swit_damp_profile",
-           "swit_forward_shot_static")
+           "swit_forward_shot_static", "swit_check")
 
 
 class SwitDesc(C.Structure):
@@ -62,6 +62,7 @@ def load(build_if_missing: bool = True):
         "swit_query": ([vp, C.POINTER(C.c_int64), C.POINTER(C.c_int32), C.POINTER(C.c_int32),
                         C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.POINTER(C.c_int32)], i),
         "swit_destroy": ([vp], i),
+        "swit_check": ([vp, vp], i),
         "swit_last_error": ([], C.c_char_p),
         "swit_damp_profile": ([C.c_int32, C.c_int32, C.c_int32, C.c_float, C.c_float, vp], i),
         "swit_forward_shot_static": ([C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_float, C.c_float, C.c_int32,

@@ -20,6 +20,7 @@
 #include "kernels_fused.cuh"
 #include "kernels_vec.cuh"
 #include "kernels_cluster.cuh"
+#include "kernels_band.cuh"
 
 using namespace swit;
 
@@ -59,7 +60,8 @@ struct swit_engine {
   int batch, bx;
   int variant;  // 1 = split, 2 = fused (one kernel per step, ping-pong), 3 = vec (split, 4 rows per thread),
                 // 4 = cluster (one persistent cluster per shot, wavefields in distributed shared memory),
-                // 5 = hybrid (cluster forward, vec reverse loop)
+                // 5 = hybrid (cluster forward, vec reverse loop), 6 = band (vec bodies on bands of
+                // columns staged through shared memory by bulk copies)
   // cluster variant: cluster sizes, threads per CTA, A and B on chip, dynamic shared memory
   int clf = 0, clb = 0, maxt_f = 0, maxt_b = 0, ab_local = 0;
   int vbx = 32;  // columns per CTA of the vec kernels (block_x for variant 3)
@@ -68,6 +70,12 @@ struct swit_engine {
   uint32_t* d_list = nullptr;
   size_t list_stride = 0;
   int list_n0[4] = {0, 0, 0, 0}, list_n1[4] = {0, 0, 0, 0}, list_len[4] = {0, 0, 0, 0};
+  // band variant: columns per band, bands, per-band task lists and counts of the four kernels
+  int band_bc = 0, nbands = 0, band_stride = 0;
+  uint32_t* d_blist = nullptr;
+  int4* d_bcnt = nullptr;
+  size_t band_sm[4] = {0, 0, 0, 0};
+  int* d_err = nullptr;  // device error word (kernels_band.cuh), read by swit_check
   size_t smf = 0, smb = 0;
   int IL;       // interior fields: row/column offset into their layout (npml for vec, else 0)
   int device;
@@ -129,7 +137,7 @@ void release(swit_engine* e) {
   void* ptrs[] = {e->d_zlo, e->d_zhi, e->d_ng, e->d_isx, e->d_isz, e->d_risx, e->d_risz, e->d_colptr, e->d_ig, e->d_zr, e->d_live,
                   e->d_mtrace, e->A, e->B, e->damp, e->cint, e->kp, e->ku, e->kw, e->p, e->u, e->w, e->pb, e->ub, e->wb, e->pe,
                   e->ue, e->we, e->dg, e->dfw, e->dbk, e->strips, e->src, e->seis_t, e->adj_t, e->d_in,
-                  e->d_stage, e->p2, e->u2, e->w2, e->pb2, e->ub2, e->wb2, e->pe2, e->ue2, e->we2, e->d_list};
+                  e->d_stage, e->p2, e->u2, e->w2, e->pb2, e->ub2, e->wb2, e->pe2, e->ue2, e->we2, e->d_list, e->d_blist, e->d_bcnt, e->d_err};
   for (void* q : ptrs)
     if (q) cudaFree(q);
 }
@@ -238,11 +246,11 @@ void launch_bwd_step(swit_engine* e, int shot0, int nb, int it, cudaStream_t st)
 // kernel's blocks may be scheduled during this one's tail and wait on chip
 // (griddepcontrol.wait in pdl_enter) until it has completed.
 template <class... P, class... A>
-void launch_pdl(bool pdl, void (*k)(P...), dim3 grid, dim3 block, cudaStream_t st, A&&... args) {
+void launch_pdl_sm(bool pdl, void (*k)(P...), dim3 grid, dim3 block, size_t smem, cudaStream_t st, A&&... args) {
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = grid;
   cfg.blockDim = block;
-  cfg.dynamicSmemBytes = 0;
+  cfg.dynamicSmemBytes = smem;
   cfg.stream = st;
   cudaLaunchAttribute at[1];
   at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
@@ -250,6 +258,16 @@ void launch_pdl(bool pdl, void (*k)(P...), dim3 grid, dim3 block, cudaStream_t s
   cfg.attrs = at;
   cfg.numAttrs = pdl ? 1 : 0;
   cudaLaunchKernelEx(&cfg, k, std::forward<A>(args)...);
+}
+template <class... P, class... A>
+void launch_pdl(bool pdl, void (*k)(P...), dim3 grid, dim3 block, cudaStream_t st, A&&... args) {
+  launch_pdl_sm(pdl, k, grid, block, 0, st, std::forward<A>(args)...);
+}
+
+// Band variant: one block per band of e->band_bc columns and shot.
+inline BandList band_list(const swit_engine* e, int k) {
+  return BandList{e->d_blist + (size_t)k * e->nbands * e->band_stride, e->d_bcnt + (size_t)k * e->nbands,
+                  e->band_stride, e->band_bc};
 }
 
 // Vec kernels: 256 threads per block over the kernel's task list k, nb shots.
@@ -307,6 +325,19 @@ void launch_forward_steps(swit_engine* e, bool store, int shot0, int nb, cudaStr
       launch_cluster_fwd_t<R, 1024>(e, store, shot0, nb, st);
     return;
   }
+  if (e->variant == 6) {
+    Grid<R> g = make_grid<R>(e);
+    R* strips = store ? (R*)e->strips : nullptr;
+    const dim3 grid(e->nbands, nb), block(256);
+    const BandList l0 = band_list(e, 0), l1 = band_list(e, 1);
+    for (int it = 2; it <= e->nt; ++it) {
+      launch_pdl_sm(e->pdl, k_fwd_p_b<R>, grid, block, e->band_sm[0], st, g, l0, make_src(e), (const R*)e->src,
+                    (R*)e->p, (const R*)e->u, (const R*)e->w, it, shot0, e->d_err);
+      launch_pdl_sm(e->pdl, k_fwd_uw_b<R>, grid, block, e->band_sm[1], st, g, l1, make_rec(e), (const R*)e->p,
+                    (R*)e->u, (R*)e->w, (R*)e->seis_t, strips, it, shot0, e->d_err);
+    }
+    return;
+  }
   if (e->variant == 3) {
     Grid<R> g = make_grid<R>(e);
     R* strips = store ? (R*)e->strips : nullptr;
@@ -344,6 +375,20 @@ void launch_backward_steps(swit_engine* e, int shot0, int nb, cudaStream_t st) {
       launch_cluster_bwd_t<R, 512>(e, shot0, nb, st);
     else
       launch_cluster_bwd_t<R, 1024>(e, shot0, nb, st);
+    return;
+  }
+  if (e->variant == 6) {
+    Grid<R> g = make_grid<R>(e);
+    const dim3 grid(e->nbands, nb), block(256);
+    const BandList l2 = band_list(e, 2), l3 = band_list(e, 3);
+    for (int it = e->nt; it >= 2; --it) {
+      launch_pdl_sm(e->pdl, k_bwd_uw_b<R>, grid, block, e->band_sm[2], st, g, l2, (const R*)e->pb, (R*)e->ub,
+                    (R*)e->wb, (const R*)e->pe, (R*)e->ue, (R*)e->we, (const R*)e->strips, it, shot0, e->d_err);
+      launch_pdl_sm(e->pdl, k_bwd_p_b<R>, grid, block, e->band_sm[3], st, g, l3, make_rec(e), make_src(e),
+                    (const R*)e->src, (const R*)e->adj_t, (R*)e->pb, (const R*)e->ub, (const R*)e->wb, (R*)e->pe,
+                    (const R*)e->ue, (const R*)e->we, (R*)e->dg, (R*)e->dfw, (R*)e->dbk, (const R*)e->strips, it,
+                    shot0, e->d_err);
+    }
     return;
   }
   if (e->variant == 3 || e->variant == 5) {
@@ -732,6 +777,18 @@ int profile_impl(swit_engine* e, int32_t launches[4], double mean_ms[4], cudaStr
         record(0);
         continue;
       }
+      if (e->variant == 6) {
+        const dim3 bg(e->nbands, nb), bb(256);
+        record(0);
+        launch_pdl_sm(false, k_fwd_p_b<R>, bg, bb, e->band_sm[0], st, g, band_list(e, 0), make_src(e),
+                      (const R*)e->src, (R*)e->p, (const R*)e->u, (const R*)e->w, it, s0, e->d_err);
+        record(0);
+        record(1);
+        launch_pdl_sm(false, k_fwd_uw_b<R>, bg, bb, e->band_sm[1], st, g, band_list(e, 1), make_rec(e),
+                      (const R*)e->p, (R*)e->u, (R*)e->w, (R*)e->seis_t, (R*)e->strips, it, s0, e->d_err);
+        record(1);
+        continue;
+      }
       if (e->variant == 3) {
         record(0);
         k_fwd_p_v<R><<<vec_grid(e, 0, nb), vec_block(e), 0, st>>>(g, vec_list(e, 0), make_src(e), (const R*)e->src,
@@ -776,6 +833,21 @@ int profile_impl(swit_engine* e, int32_t launches[4], double mean_ms[4], cudaStr
         record(2);
         launch_bwd_step<R>(e, s0, nb, it, st);
         record(2);
+        continue;
+      }
+      if (e->variant == 6) {
+        const dim3 bg(e->nbands, nb), bb(256);
+        record(2);
+        launch_pdl_sm(false, k_bwd_uw_b<R>, bg, bb, e->band_sm[2], st, g, band_list(e, 2), (const R*)e->pb,
+                      (R*)e->ub, (R*)e->wb, (const R*)e->pe, (R*)e->ue, (R*)e->we, (const R*)e->strips, it, s0,
+                      e->d_err);
+        record(2);
+        record(3);
+        launch_pdl_sm(false, k_bwd_p_b<R>, bg, bb, e->band_sm[3], st, g, band_list(e, 3), make_rec(e), make_src(e),
+                      (const R*)e->src, (const R*)e->adj_t, (R*)e->pb, (const R*)e->ub, (const R*)e->wb, (R*)e->pe,
+                      (const R*)e->ue, (const R*)e->we, (R*)e->dg, (R*)e->dfw, (R*)e->dbk, (const R*)e->strips, it,
+                      s0, e->d_err);
+        record(3);
         continue;
       }
       if (e->variant == 3 || e->variant == 5) {
@@ -861,16 +933,25 @@ int import_impl(swit_engine* e, const float* src, const float* boundary, const f
 // tiles of 256/vbx vectors x vbx columns, q fastest, so a warp covers
 // 32 * vbx / 256 columns of 256 / vbx vectors as a 2-D block of the grid would.
 template <class R>
-int build_lists(swit_engine* e) {
-  const int LD4 = e->LD / 4, NX = e->NX;
-  const size_t n = (size_t)NX * LD4;
+int vector_tiers(swit_engine* e, std::vector<int>& t) {
+  const size_t n = (size_t)e->NX * (e->LD / 4);
   int* d_t = nullptr;
   CK(cudaMalloc(&d_t, 4 * n * sizeof(int)));
   k_tiers<R><<<nblocks(n), 256>>>(make_grid<R>(e), make_src(e), make_rec(e), e->ns, d_t);
-  std::vector<int> t(4 * n);
+  t.resize(4 * n);
   cudaError_t ce = cudaMemcpy(t.data(), d_t, 4 * n * sizeof(int), cudaMemcpyDeviceToHost);
   cudaFree(d_t);
   if (ce != cudaSuccess) return fail(SWIT_E_CUDA, "task tiers: %s", cudaGetErrorString(ce));
+  return 0;
+}
+
+template <class R>
+int build_lists(swit_engine* e) {
+  const int LD4 = e->LD / 4, NX = e->NX;
+  const size_t n = (size_t)NX * LD4;
+  std::vector<int> t;
+  int rt = vector_tiers<R>(e, t);
+  if (rt) return rt;
   const int TX = e->vbx, TQ = 256 / e->vbx;
   std::vector<uint32_t> L(4 * n);
   for (int k = 0; k < 4; ++k) {
@@ -892,6 +973,76 @@ int build_lists(swit_engine* e) {
   int rc = dalloc(e, &e->d_list, 4 * n);
   if (rc) return rc;
   CK(cudaMemcpy(e->d_list, L.data(), 4 * n * sizeof(uint32_t), cudaMemcpyHostToDevice));
+  return 0;
+}
+
+// Band variant: per kernel and band of band_bc columns, the band's vectors by
+// body tier (no-work vectors dropped), column-major within a tier; counts
+// {first tier-1 entry, first tier-2 entry, length}.  Also sets the kernels'
+// shared-memory sizes.
+template <class R>
+int build_band_lists(swit_engine* e) {
+  const int LD4 = e->LD / 4, NX = e->NX, bc = e->band_bc;
+  const size_t n = (size_t)NX * LD4;
+  std::vector<int> t;
+  int rt = vector_tiers<R>(e, t);
+  if (rt) return rt;
+  e->nbands = (NX + bc - 1) / bc;
+  e->band_stride = bc * LD4;
+  const size_t per = (size_t)e->nbands * e->band_stride;
+  std::vector<uint32_t> L(4 * per, 0u);
+  std::vector<int4> cnt(4 * (size_t)e->nbands);
+  for (int k = 0; k < 4; ++k) {
+    const int* tk = &t[k * n];
+    for (int b = 0; b < e->nbands; ++b) {
+      uint32_t* out = &L[k * per + (size_t)b * e->band_stride];
+      int m = 0, n0 = 0, n1 = 0;
+      for (int tier = 0; tier < 3; ++tier) {
+        if (tier == 1) n0 = m;
+        if (tier == 2) n1 = m;
+        for (int x = b * bc; x < std::min((b + 1) * bc, NX); ++x)
+          for (int q = 0; q < LD4; ++q)
+            if (tk[(size_t)x * LD4 + q] == tier) out[m++] = ((uint32_t)(x - b * bc) << 16) | (uint32_t)q;
+      }
+      cnt[k * (size_t)e->nbands + b] = make_int4(n0, n1, m, 0);
+    }
+  }
+  int rc = dalloc(e, &e->d_blist, 4 * per);
+  if (!rc) rc = dalloc(e, &e->d_bcnt, 4 * (size_t)e->nbands);
+  if (rc) return rc;
+  CK(cudaMemcpy(e->d_blist, L.data(), L.size() * sizeof(uint32_t), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(e->d_bcnt, cnt.data(), cnt.size() * sizeof(int4), cudaMemcpyHostToDevice));
+  return 0;
+}
+
+// Band variant geometry: columns per band (want, or as many as 256 threads
+// cover), shared memory of each kernel checked against the device limit.
+template <class R>
+int setup_band(swit_engine* e, int want) {
+  int dev = 0, optin = 0;
+  cudaGetDevice(&dev);
+  if (cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess || optin <= 0)
+    return fail(SWIT_E_CUDA, "cannot query the shared memory per block");
+  const int LD4 = e->LD / 4;
+  if (want < 0 || want > 64) return fail(SWIT_E_ARG, "block_x of the band kernels (columns per band) must be 0..64");
+  const int bc = want ? want : std::max(1, 256 / LD4);
+  e->band_bc = bc;
+  e->bx = bc;
+  e->band_sm[0] = band_smem(bc, e->LD, 1, 4, e->esz);
+  e->band_sm[1] = band_smem(bc, e->LD, 1, 5, e->esz);
+  e->band_sm[2] = band_smem(bc, e->LD, 2, 8, e->esz);
+  e->band_sm[3] = band_smem(bc, e->LD, 2, 10, e->esz);
+  for (size_t b : e->band_sm)
+    if (b + 64 > (size_t)optin)
+      return fail(SWIT_E_LIMIT, "a band of %d columns needs %zu bytes of shared memory per block (> %d)", bc, b, optin);
+  cudaError_t rc = cudaFuncSetAttribute(k_fwd_p_b<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)e->band_sm[0]);
+  if (rc == cudaSuccess)
+    rc = cudaFuncSetAttribute(k_fwd_uw_b<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)e->band_sm[1]);
+  if (rc == cudaSuccess)
+    rc = cudaFuncSetAttribute(k_bwd_uw_b<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)e->band_sm[2]);
+  if (rc == cudaSuccess)
+    rc = cudaFuncSetAttribute(k_bwd_p_b<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)e->band_sm[3]);
+  if (rc != cudaSuccess) return fail(SWIT_E_CUDA, "band kernel attributes: %s", cudaGetErrorString(rc));
   return 0;
 }
 
@@ -1014,9 +1165,9 @@ int swit_create(const swit_desc* d, swit_engine** out) {
   e->dt32 = d->dt;
   e->esz = e->prec ? sizeof(double) : sizeof(float);
   e->batch = d->shots_per_batch > 0 ? std::min(d->shots_per_batch, d->ns) : d->ns;
-  if (d->kernel_variant < 0 || d->kernel_variant > 5) {
+  if (d->kernel_variant < 0 || d->kernel_variant > 6) {
     delete e;
-    return fail(SWIT_E_ARG, "kernel_variant must be 0..5");
+    return fail(SWIT_E_ARG, "kernel_variant must be 0..6");
   }
   e->variant = d->kernel_variant ? d->kernel_variant : 3;
   if (e->variant == 2 && e->LD > 1024) {
@@ -1028,6 +1179,12 @@ int swit_create(const swit_desc* d, swit_engine** out) {
     if (e->bx != 8 && e->bx != 16 && e->bx != 32) {
       delete e;
       return fail(SWIT_E_ARG, "block_x of the fused kernels must be 8, 16 or 32");
+    }
+  } else if (e->variant == 6) {
+    int rc6 = e->prec ? setup_band<double>(e, d->block_x) : setup_band<float>(e, d->block_x);
+    if (rc6) {
+      delete e;
+      return rc6;
     }
   } else if (e->variant == 4 || e->variant == 5) {
     int rc4 = e->prec ? setup_cluster<double>(e, d->block_x) : setup_cluster<float>(e, d->block_x);
@@ -1146,6 +1303,7 @@ int swit_create(const swit_desc* d, swit_engine** out) {
   AL(dalloc(e, &e->d_zr, nent));
   AL(dalloc(e, &e->d_live, (size_t)ns * ngm));
   AL(dalloc(e, &e->d_mtrace, (size_t)ns * ngm));
+  AL(dalloc(e, &e->d_err, 1));
   AL(valloc(e, &e->A, FSZ));
   AL(valloc(e, &e->B, FSZ));
   AL(valloc(e, &e->damp, (size_t)L + 1));
@@ -1188,6 +1346,14 @@ int swit_create(const swit_desc* d, swit_engine** out) {
     delete e;
     return rc;
   }
+  if (e->variant == 6) {
+    rc = e->prec ? build_band_lists<double>(e) : build_band_lists<float>(e);
+    if (rc) {
+      release(e);
+      delete e;
+      return rc;
+    }
+  }
   if (e->variant == 3 || e->variant == 5) {
     rc = e->prec ? build_lists<double>(e) : build_lists<float>(e);
     if (rc) {
@@ -1200,6 +1366,7 @@ int swit_create(const swit_desc* d, swit_engine** out) {
   // seismograms (fdcore.f90 starts at it = 2), traces beyond ng(is), and the
   // strips of step 1 that the reconstruction inserts at it = 2.
   cudaError_t ce = cudaMemset(e->seis_t, 0, (size_t)ns * e->nt * ngm * e->esz);
+  if (ce == cudaSuccess) ce = cudaMemset(e->d_err, 0, sizeof(int));
   if (ce == cudaSuccess) ce = cudaMemset(e->strips, 0, (size_t)ns * e->nt * e->SL * e->esz);
   if (ce == cudaSuccess) ce = cudaMemset(e->adj_t, 0, (size_t)ns * e->nt * ngm * e->esz);
   if (ce == cudaSuccess) ce = cudaStreamCreateWithFlags(&e->cap, cudaStreamNonBlocking);
@@ -1213,7 +1380,7 @@ int swit_create(const swit_desc* d, swit_engine** out) {
   const int per = e->path == 1 ? ns : waves;
   const int per_step = e->variant == 2 ? 1 : 2;
   const int fwaves = e->path == 1 ? ns : (ns + fwd_batch(e) - 1) / fwd_batch(e);
-  e->launches_fwd = e->variant >= 4 ? fwaves : per * (e->nt - 1) * per_step;
+  e->launches_fwd = (e->variant == 4 || e->variant == 5) ? fwaves : per * (e->nt - 1) * per_step;
   e->launches_bwd = e->variant == 4 ? per : per * (e->nt - 1) * per_step;
   *out = e;
   return 0;
@@ -1305,6 +1472,18 @@ int swit_query(const swit_engine* e, int64_t* device_bytes, int32_t* shots_per_b
   if (kernels_per_forward) *kernels_per_forward = e->launches_fwd;
   if (kernels_per_backward) *kernels_per_backward = e->launches_bwd;
   if (kernel_variant) *kernel_variant = e->variant;
+  return 0;
+}
+
+int swit_check(swit_engine* e, void* stream) {
+  if (!e) return fail(SWIT_E_ARG, "null engine");
+  CK(cudaStreamSynchronize((cudaStream_t)stream));
+  int w = 0;
+  CK(cudaMemcpy(&w, e->d_err, sizeof(int), cudaMemcpyDeviceToHost));
+  if (w) {
+    CK(cudaMemset(e->d_err, 0, sizeof(int)));
+    return fail(SWIT_E_TIMEOUT, "a kernel gave up waiting for its staged copies (error word %d); results are invalid", w);
+  }
   return 0;
 }
 

@@ -45,7 +45,7 @@ class Engine:
         if path not in ("batched", "plain"):
             raise ValueError("path must be 'batched' or 'plain'")
         self.path = path
-        variants = {"auto": 0, "split": 1, "fused": 2, "vec": 3, "cluster": 4, "hybrid": 5}
+        variants = {"auto": 0, "split": 1, "fused": 2, "vec": 3, "cluster": 4, "hybrid": 5, "band": 6}
         if kernel not in variants:
             raise ValueError("kernel must be one of %s" % ", ".join(sorted(variants)))
         self._keep = dict(
@@ -193,7 +193,13 @@ class Engine:
         _lib.check(self._lib.swit_query(self._h, C.byref(by), C.byref(sb), C.byref(bx), C.byref(kf), C.byref(kb),
                                         C.byref(kv)))
         return dict(device_bytes=by.value, shots_per_batch=sb.value, block_x=bx.value, kernels_per_forward=kf.value,
-                    kernels_per_backward=kb.value, kernel={1: "split", 2: "fused", 3: "vec", 4: "cluster", 5: "hybrid"}.get(kv.value, "?"))
+                    kernels_per_backward=kb.value, kernel={1: "split", 2: "fused", 3: "vec", 4: "cluster", 5: "hybrid", 6: "band"}.get(kv.value, "?"))
+
+    def check(self):
+        """Waits for torch's current stream and raises SwitError if a kernel gave
+        up waiting on an in-kernel copy since the last check (swit_check)."""
+        import torch
+        _lib.check(self._lib.swit_check(self._h, torch.cuda.current_stream().cuda_stream))
 
     def close(self):
         if getattr(self, "_h", None):

@@ -56,7 +56,7 @@ def test_forward_seismograms_match_oracle(base):
     np.testing.assert_array_equal(seis, base["ref"]["seis"])
 
 
-@pytest.mark.parametrize("kernel", ["split", "vec", "cluster"])
+@pytest.mark.parametrize("kernel", ["split", "vec", "cluster", "band"])
 def test_boundary_strips_and_end_states_match_oracle(base, kernel):
     s = base["s"]
     with engine(s, kernel=kernel) as e:
@@ -106,19 +106,22 @@ def test_gradient_l2_single_call_matches_oracle(base):
                                   dict(kernel="cluster", block_x=7), dict(kernel="cluster", path="plain"),
                                   dict(kernel="cluster", shots_per_batch=2), dict(kernel="hybrid"),
                                   dict(kernel="hybrid", block_x=3, shots_per_batch=2),
-                                  dict(kernel="hybrid", path="plain")])
+                                  dict(kernel="hybrid", path="plain"), dict(kernel="band"),
+                                  dict(kernel="band", block_x=1), dict(kernel="band", block_x=3),
+                                  dict(kernel="band", block_x=7, shots_per_batch=2), dict(kernel="band", path="plain")])
 def test_launch_variants_are_identical(base, opts):
     s = base["s"]
     with engine(s, **opts) as e:
         e.set_model(s.vp_true, base["rho"])
         seis = e.forward(base["src"], save_boundary=True)
         g, fw, bk = e.backward(base["adj"])
+        e.check()
     np.testing.assert_array_equal(seis, base["ref"]["seis"])
     np.testing.assert_array_equal(g, base["grad"]["g"])
     np.testing.assert_array_equal(bk, base["grad"]["bk"])
 
 
-@pytest.mark.parametrize("kernel", ["fused", "split", "vec", "cluster"])
+@pytest.mark.parametrize("kernel", ["fused", "split", "vec", "cluster", "band"])
 def test_fp64_build_matches_fp64_oracle(base, kernel):
     s, pb = base["s"], base["pb"]
     ref = O.forward(pb, s.vp_true, base["rho"], base["src"], store=True, fp64=True)
@@ -143,7 +146,7 @@ def test_repeated_backward_after_one_forward(base):
     np.testing.assert_array_equal(g2, base["grad"]["g"])
 
 
-@pytest.mark.parametrize("kernel", ["fused", "split", "vec", "cluster"])
+@pytest.mark.parametrize("kernel", ["fused", "split", "vec", "cluster", "band"])
 def test_edge_geometry_surface_receivers_deep_source_uneven_traces(kernel):
     """Receivers on z = 0 (moved one node down), a source deep enough that the
     reconstruction subtracts it (fdcore.f90:250-256), shots with different
@@ -171,7 +174,7 @@ def test_edge_geometry_surface_receivers_deep_source_uneven_traces(kernel):
     np.testing.assert_array_equal(bk, gref["bk"])
 
 
-@pytest.mark.parametrize("kernel", ["fused", "split", "vec", "cluster"])
+@pytest.mark.parametrize("kernel", ["fused", "split", "vec", "cluster", "band"])
 def test_no_free_surface(kernel):
     s, _ = case(nt=200)
     s.free_surface = 0
@@ -220,7 +223,7 @@ def test_state_and_model_errors(base):
             e.backward(base["adj"])
 
 
-@pytest.mark.parametrize("kernel", ["vec", "cluster"])
+@pytest.mark.parametrize("kernel", ["vec", "cluster", "band"])
 @pytest.mark.parametrize("npml", [8, 9, 10, 11])
 def test_vec_kernels_every_mirror_alignment(npml, kernel):
     """The vectorised kernels own 4 rows per thread; npml mod 4 decides whether
@@ -242,7 +245,7 @@ def test_vec_kernels_every_mirror_alignment(npml, kernel):
     np.testing.assert_array_equal(bk, gref["bk"])
 
 
-@pytest.mark.parametrize("kernel", ["vec", "split", "fused", "cluster"])
+@pytest.mark.parametrize("kernel", ["vec", "split", "fused", "cluster", "band"])
 def test_import_snapshot_replaces_the_forward_run(base, kernel):
     """The adjoint job from saved files (fd2dmpi/solver.f90:212-228): export the
     strips and end states, load them into a fresh engine, run only the reverse loop."""
