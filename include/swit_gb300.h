@@ -92,6 +92,15 @@ typedef struct swit_desc {
                                6 = band: the vec bodies on bands of block_x
                                columns (0 = as many as 256 threads cover) staged
                                through shared memory by bulk copies            */
+  int32_t checkpoint_every; /* 0 = boundary saving (fd2dmpi's strategy: strips of
+                               every step, ns*nt*(9nx+6nz) values); k > 0 =
+                               checkpointed recomputation (vec and band kernels):
+                               the forward keeps the full state every k steps, the
+                               reverse loop re-runs each k-step segment from its
+                               checkpoint to regenerate that segment's strips.
+                               Same results bit for bit; about one more forward
+                               pass of work; export/import of snapshots and
+                               swit_profile_kernels need k = 0                 */
 } swit_desc;
 
 /* Creates an engine and allocates its device workspace on the current device.

@@ -25,7 +25,7 @@ class SwitDesc(C.Structure):
                 ("ng_max", C.c_int32), ("ng", C.c_void_p), ("src_x", C.c_void_p), ("src_z", C.c_void_p),
                 ("rec_x", C.c_void_p), ("rec_z", C.c_void_p), ("precision", C.c_int32), ("path", C.c_int32),
                 ("shots_per_batch", C.c_int32), ("block_x", C.c_int32),
-                ("kernel_variant", C.c_int32)]
+                ("kernel_variant", C.c_int32), ("checkpoint_every", C.c_int32)]
 
 
 class SwitError(RuntimeError):

@@ -76,6 +76,10 @@ struct swit_engine {
   int4* d_bcnt = nullptr;
   size_t band_sm[4] = {0, 0, 0, 0};
   int* d_err = nullptr;  // device error word (kernels_band.cuh), read by swit_check
+  // checkpointed recomputation: every ckpt_k steps, ckpt_m segments; strip buffer of snt steps per shot whose
+  // slot 0 holds step sit0; ckpt = ckpt_m slots x {p, u, w} x ns x FSZ (slot m: state after segment m)
+  int ckpt_k = 0, ckpt_m = 0, snt = 0, sit0 = 1;
+  void* ckpt = nullptr;
   size_t smf = 0, smb = 0;
   int IL;       // interior fields: row/column offset into their layout (npml for vec, else 0)
   int device;
@@ -137,7 +141,7 @@ void release(swit_engine* e) {
   void* ptrs[] = {e->d_zlo, e->d_zhi, e->d_ng, e->d_isx, e->d_isz, e->d_risx, e->d_risz, e->d_colptr, e->d_ig, e->d_zr, e->d_live,
                   e->d_mtrace, e->A, e->B, e->damp, e->cint, e->kp, e->ku, e->kw, e->p, e->u, e->w, e->pb, e->ub, e->wb, e->pe,
                   e->ue, e->we, e->dg, e->dfw, e->dbk, e->strips, e->src, e->seis_t, e->adj_t, e->d_in,
-                  e->d_stage, e->p2, e->u2, e->w2, e->pb2, e->ub2, e->wb2, e->pe2, e->ue2, e->we2, e->d_list, e->d_blist, e->d_bcnt, e->d_err};
+                  e->d_stage, e->p2, e->u2, e->w2, e->pb2, e->ub2, e->wb2, e->pe2, e->ue2, e->we2, e->d_list, e->d_blist, e->d_bcnt, e->d_err, e->ckpt};
   for (void* q : ptrs)
     if (q) cudaFree(q);
 }
@@ -157,6 +161,8 @@ Grid<R> make_grid(const swit_engine* e) {
   g.nt = e->nt;
   g.ngmax = e->ngmax;
   g.SL = e->SL;
+  g.snt = e->snt;
+  g.sit0 = e->sit0;
   g.FSZ = (size_t)e->NX * e->LD;
   g.FSI = e->variant >= 3 ? g.FSZ : (size_t)e->nx * e->LDI;
   g.IL = e->IL;
@@ -317,7 +323,9 @@ void launch_cluster_bwd_t(swit_engine* e, int shot0, int nb, cudaStream_t st) {
 
 // Forward time loop of shots [shot0, shot0+nb): fdcore.f90:75-160.
 template <class R>
-void launch_forward_steps(swit_engine* e, bool store, int shot0, int nb, cudaStream_t st) {
+void launch_forward_steps(swit_engine* e, bool store, int shot0, int nb, cudaStream_t st, int it_lo = 2,
+                          int it_hi = -1) {
+  if (it_hi < 0) it_hi = e->nt;
   if (e->variant == 4 || e->variant == 5) {
     if (e->maxt_f == 512)
       launch_cluster_fwd_t<R, 512>(e, store, shot0, nb, st);
@@ -330,7 +338,7 @@ void launch_forward_steps(swit_engine* e, bool store, int shot0, int nb, cudaStr
     R* strips = store ? (R*)e->strips : nullptr;
     const dim3 grid(e->nbands, nb), block(256);
     const BandList l0 = band_list(e, 0), l1 = band_list(e, 1);
-    for (int it = 2; it <= e->nt; ++it) {
+    for (int it = it_lo; it <= it_hi; ++it) {
       launch_pdl_sm(e->pdl, k_fwd_p_b<R>, grid, block, e->band_sm[0], st, g, l0, make_src(e), (const R*)e->src,
                     (R*)e->p, (const R*)e->u, (const R*)e->w, it, shot0, e->d_err);
       launch_pdl_sm(e->pdl, k_fwd_uw_b<R>, grid, block, e->band_sm[1], st, g, l1, make_rec(e), (const R*)e->p,
@@ -343,7 +351,7 @@ void launch_forward_steps(swit_engine* e, bool store, int shot0, int nb, cudaStr
     R* strips = store ? (R*)e->strips : nullptr;
     const dim3 block = vec_block(e), g0 = vec_grid(e, 0, nb), g1 = vec_grid(e, 1, nb);
     const VecList l0 = vec_list(e, 0), l1 = vec_list(e, 1);
-    for (int it = 2; it <= e->nt; ++it) {
+    for (int it = it_lo; it <= it_hi; ++it) {
       launch_pdl(e->pdl, k_fwd_p_v<R>, g0, block, st, g, l0, make_src(e), (const R*)e->src, (R*)e->p,
                  (const R*)e->u, (const R*)e->w, it, shot0);
       launch_pdl(e->pdl, k_fwd_uw_v<R>, g1, block, st, g, l1, make_rec(e), (const R*)e->p, (R*)e->u, (R*)e->w,
@@ -352,14 +360,14 @@ void launch_forward_steps(swit_engine* e, bool store, int shot0, int nb, cudaStr
     return;
   }
   if (e->variant == 2) {
-    for (int it = 2; it <= e->nt; ++it) launch_fwd_step<R>(e, store, shot0, nb, it, st);
+    for (int it = it_lo; it <= it_hi; ++it) launch_fwd_step<R>(e, store, shot0, nb, it, st);
     return;
   }
   Grid<R> g = make_grid<R>(e);
   dim3 grid, block;
   stencil_shape(e, nb, grid, block);
   R* strips = store ? (R*)e->strips : nullptr;
-  for (int it = 2; it <= e->nt; ++it) {
+  for (int it = it_lo; it <= it_hi; ++it) {
     k_fwd_p<R><<<grid, block, 0, st>>>(g, make_src(e), (const R*)e->src, (R*)e->p, (const R*)e->u, (const R*)e->w, it,
                                        shot0);
     k_fwd_uw<R><<<grid, block, 0, st>>>(g, make_rec(e), (const R*)e->p, (R*)e->u, (R*)e->w, (R*)e->seis_t, strips, it,
@@ -369,7 +377,8 @@ void launch_forward_steps(swit_engine* e, bool store, int shot0, int nb, cudaStr
 
 // Reverse time loop of shots [shot0, shot0+nb): solver.f90:230-253.
 template <class R>
-void launch_backward_steps(swit_engine* e, int shot0, int nb, cudaStream_t st) {
+void launch_backward_steps(swit_engine* e, int shot0, int nb, cudaStream_t st, int it_hi = -1, int it_lo = 2) {
+  if (it_hi < 0) it_hi = e->nt;
   if (e->variant == 4) {
     if (e->maxt_b == 512)
       launch_cluster_bwd_t<R, 512>(e, shot0, nb, st);
@@ -381,7 +390,7 @@ void launch_backward_steps(swit_engine* e, int shot0, int nb, cudaStream_t st) {
     Grid<R> g = make_grid<R>(e);
     const dim3 grid(e->nbands, nb), block(256);
     const BandList l2 = band_list(e, 2), l3 = band_list(e, 3);
-    for (int it = e->nt; it >= 2; --it) {
+    for (int it = it_hi; it >= it_lo; --it) {
       launch_pdl_sm(e->pdl, k_bwd_uw_b<R>, grid, block, e->band_sm[2], st, g, l2, (const R*)e->pb, (R*)e->ub,
                     (R*)e->wb, (const R*)e->pe, (R*)e->ue, (R*)e->we, (const R*)e->strips, it, shot0, e->d_err);
       launch_pdl_sm(e->pdl, k_bwd_p_b<R>, grid, block, e->band_sm[3], st, g, l3, make_rec(e), make_src(e),
@@ -395,7 +404,7 @@ void launch_backward_steps(swit_engine* e, int shot0, int nb, cudaStream_t st) {
     Grid<R> g = make_grid<R>(e);
     const dim3 block = vec_block(e), g2 = vec_grid(e, 2, nb), g3 = vec_grid(e, 3, nb);
     const VecList l2 = vec_list(e, 2), l3 = vec_list(e, 3);
-    for (int it = e->nt; it >= 2; --it) {
+    for (int it = it_hi; it >= it_lo; --it) {
       launch_pdl(e->pdl, k_bwd_uw_v<R>, g2, block, st, g, l2, (const R*)e->pb, (R*)e->ub, (R*)e->wb,
                  (const R*)e->pe, (R*)e->ue, (R*)e->we, (const R*)e->strips, it, shot0);
       launch_pdl(e->pdl, k_bwd_p_v<R>, g3, block, st, g, l3, make_rec(e), make_src(e), (const R*)e->src,
@@ -405,13 +414,13 @@ void launch_backward_steps(swit_engine* e, int shot0, int nb, cudaStream_t st) {
     return;
   }
   if (e->variant == 2) {
-    for (int it = e->nt; it >= 2; --it) launch_bwd_step<R>(e, shot0, nb, it, st);
+    for (int it = it_hi; it >= it_lo; --it) launch_bwd_step<R>(e, shot0, nb, it, st);
     return;
   }
   Grid<R> g = make_grid<R>(e);
   dim3 grid, block;
   stencil_shape(e, nb, grid, block);
-  for (int it = e->nt; it >= 2; --it) {
+  for (int it = it_hi; it >= it_lo; --it) {
     k_bwd_uw<R><<<grid, block, 0, st>>>(g, (const R*)e->pb, (R*)e->ub, (R*)e->wb, (const R*)e->pe, (R*)e->ue,
                                         (R*)e->we, (const R*)e->strips, it, shot0);
     k_bwd_p<R><<<grid, block, 0, st>>>(g, make_rec(e), make_src(e), (const R*)e->src, (const R*)e->adj_t, (R*)e->pb,
@@ -425,10 +434,68 @@ void launch_backward_steps(swit_engine* e, int shot0, int nb, cudaStream_t st) {
 // launch (the hardware schedules the clusters); the others use the batch.
 inline int fwd_batch(const swit_engine* e) { return e->variant == 5 ? e->ns : e->batch; }
 
+// Checkpointed recomputation.  Segment m (m = 0 .. ckpt_m-1, ckpt_m =
+// ceil(nt/k)) is the forward steps [max(2, m k + 1), min(nt, (m+1) k)]; the
+// reverse steps that read its strips are [m k + 2, min(nt, (m+1) k + 1)]
+// (reverse step it reads the strips of step it-1; none for the last segment
+// when m k + 2 > nt).  Checkpoint slot m holds (p, u, w) after segment m (the
+// last slot is the final state); the state before segment 0 is zero.
+inline void ckpt_copy(swit_engine* e, int slot, int s0, int nb, bool save, cudaStream_t st) {
+  const size_t fsz = (size_t)e->NX * e->LD * e->esz;
+  void* f[3] = {e->p, e->u, e->w};
+  for (int q = 0; q < 3; ++q) {
+    char* c = (char*)e->ckpt + (((size_t)slot * 3 + q) * e->ns + s0) * fsz;
+    char* a = (char*)f[q] + (size_t)s0 * fsz;
+    cudaMemcpyAsync(save ? c : a, save ? a : c, (size_t)nb * fsz, cudaMemcpyDeviceToDevice, st);
+  }
+}
+
+// Forward of shots [s0, s0+nb) keeping checkpoints instead of strips.
+template <class R>
+void forward_checkpointed(swit_engine* e, int s0, int nb, cudaStream_t st) {
+  const int k = e->ckpt_k;
+  for (int m = 0; m < e->ckpt_m; ++m) {
+    launch_forward_steps<R>(e, false, s0, nb, st, std::max(2, m * k + 1), std::min(e->nt, (m + 1) * k));
+    ckpt_copy(e, m, s0, nb, true, st);
+  }
+}
+
+// Reverse loop of shots [s0, s0+nb): per segment, last first, restore the
+// state before it, re-run its forward steps into the k-step strip buffer
+// (the same kernels, so the same strips as a boundary-saving run), then run
+// the reverse steps that read them.  Leaves sit0 = 1.
+template <class R>
+void backward_checkpointed(swit_engine* e, int s0, int nb, cudaStream_t st) {
+  const int k = e->ckpt_k;
+  const size_t fsz = (size_t)e->NX * e->LD * e->esz;
+  for (int m = e->ckpt_m - 1; m >= 0; --m) {
+    if (m * k + 2 > e->nt) continue;
+    if (m > 0) {
+      ckpt_copy(e, m - 1, s0, nb, false, st);
+    } else {
+      cudaMemsetAsync((char*)e->p + (size_t)s0 * fsz, 0, (size_t)nb * fsz, st);
+      cudaMemsetAsync((char*)e->u + (size_t)s0 * fsz, 0, (size_t)nb * fsz, st);
+      cudaMemsetAsync((char*)e->w + (size_t)s0 * fsz, 0, (size_t)nb * fsz, st);
+      // the strips of step 1 (slot 0 of segment 0) are zero: no forward step 1 runs
+      cudaMemsetAsync((char*)e->strips + (size_t)s0 * e->snt * e->SL * e->esz, 0,
+                      (size_t)nb * e->snt * e->SL * e->esz, st);
+    }
+    e->sit0 = m * k + 1;
+    launch_forward_steps<R>(e, true, s0, nb, st, std::max(2, m * k + 1), std::min(e->nt, (m + 1) * k));
+    launch_backward_steps<R>(e, s0, nb, st, std::min(e->nt, (m + 1) * k + 1), m * k + 2);
+  }
+  e->sit0 = 1;
+}
+
 template <class R>
 int run_forward_loop(swit_engine* e, bool store, cudaStream_t st) {
   if (e->path == 1) {
-    for (int s = 0; s < e->ns; ++s) launch_forward_steps<R>(e, store, s, 1, st);
+    for (int s = 0; s < e->ns; ++s) {
+      if (store && e->ckpt_k)
+        forward_checkpointed<R>(e, s, 1, st);
+      else
+        launch_forward_steps<R>(e, store, s, 1, st);
+    }
     CK(cudaGetLastError());
     return 0;
   }
@@ -437,7 +504,12 @@ int run_forward_loop(swit_engine* e, bool store, cudaStream_t st) {
     cudaGraph_t graph;
     CK(cudaStreamBeginCapture(e->cap, cudaStreamCaptureModeThreadLocal));
     const int fb = fwd_batch(e);
-    for (int s0 = 0; s0 < e->ns; s0 += fb) launch_forward_steps<R>(e, store, s0, std::min(fb, e->ns - s0), e->cap);
+    for (int s0 = 0; s0 < e->ns; s0 += fb) {
+      if (store && e->ckpt_k)
+        forward_checkpointed<R>(e, s0, std::min(fb, e->ns - s0), e->cap);
+      else
+        launch_forward_steps<R>(e, store, s0, std::min(fb, e->ns - s0), e->cap);
+    }
     cudaError_t rc = cudaStreamEndCapture(e->cap, &graph);
     if (rc != cudaSuccess) return fail(SWIT_E_CUDA, "forward graph capture: %s", cudaGetErrorString(rc));
     rc = cudaGraphInstantiate(&ex, graph, 0);
@@ -454,14 +526,24 @@ int run_forward_loop(swit_engine* e, bool store, cudaStream_t st) {
 template <class R>
 int run_backward_loop(swit_engine* e, cudaStream_t st) {
   if (e->path == 1) {
-    for (int s = 0; s < e->ns; ++s) launch_backward_steps<R>(e, s, 1, st);
+    for (int s = 0; s < e->ns; ++s) {
+      if (e->ckpt_k)
+        backward_checkpointed<R>(e, s, 1, st);
+      else
+        launch_backward_steps<R>(e, s, 1, st);
+    }
     CK(cudaGetLastError());
     return 0;
   }
   if (!e->gbwd) {
     cudaGraph_t graph;
     CK(cudaStreamBeginCapture(e->cap, cudaStreamCaptureModeThreadLocal));
-    for (int s0 = 0; s0 < e->ns; s0 += e->batch) launch_backward_steps<R>(e, s0, std::min(e->batch, e->ns - s0), e->cap);
+    for (int s0 = 0; s0 < e->ns; s0 += e->batch) {
+      if (e->ckpt_k)
+        backward_checkpointed<R>(e, s0, std::min(e->batch, e->ns - s0), e->cap);
+      else
+        launch_backward_steps<R>(e, s0, std::min(e->batch, e->ns - s0), e->cap);
+    }
     cudaError_t rc = cudaStreamEndCapture(e->cap, &graph);
     if (rc != cudaSuccess) return fail(SWIT_E_CUDA, "backward graph capture: %s", cudaGetErrorString(rc));
     rc = cudaGraphInstantiate(&e->gbwd, graph, 0);
@@ -494,6 +576,13 @@ void copy_end(swit_engine* e, cudaStream_t st) {
   const R* P = (const R*)(in_b ? e->p2 : e->p);
   const R* U = (const R*)(in_b ? e->u2 : e->u);
   const R* W = (const R*)(in_b ? e->w2 : e->w);
+  if (e->ckpt_k) {  // the reverse loop reuses p, u, w; the final state is checkpoint slot ckpt_m-1
+    const size_t f = (size_t)e->ns * e->NX * e->LD;
+    const R* c = (const R*)e->ckpt + (size_t)(e->ckpt_m - 1) * 3 * f;
+    P = c;
+    U = c + f;
+    W = c + 2 * f;
+  }
   k_copy_end<R><<<nblocks((size_t)e->ns * e->nx * e->nz), 256, 0, st>>>(g, P, U, W, (R*)e->pe, (R*)e->ue,
                                                                         (R*)e->we, e->ns);
 }
@@ -702,6 +791,7 @@ int set_model_impl(swit_engine* e, const float* vp, const float* rho, cudaStream
 
 template <class R>
 int export_impl(swit_engine* e, void* boundary, void* pend, void* uend, void* wend, int on_device, cudaStream_t st) {
+  if (e->ckpt_k) return fail(SWIT_E_STATE, "this call needs boundary saving (checkpoint_every = 0)");
   Grid<R> g = make_grid<R>(e);
   copy_end<R>(e, st);
   const size_t NB = (size_t)e->ns * e->nt * e->SL, NI = (size_t)e->ns * e->nx * e->nz;
@@ -746,6 +836,7 @@ int export_impl(swit_engine* e, void* boundary, void* pend, void* uend, void* we
 // Per-launch timing of the stencil kernels with CUDA events.
 template <class R>
 int profile_impl(swit_engine* e, int32_t launches[4], double mean_ms[4], cudaStream_t st) {
+  if (e->ckpt_k) return fail(SWIT_E_STATE, "this call needs boundary saving (checkpoint_every = 0)");
   Grid<R> g = make_grid<R>(e);
   const int nshot_launch = e->path == 1 ? 1 : e->batch;
   std::vector<cudaEvent_t> ev[4];
@@ -897,6 +988,7 @@ int profile_impl(swit_engine* e, int32_t launches[4], double mean_ms[4], cudaStr
 template <class R>
 int import_impl(swit_engine* e, const float* src, const float* boundary, const float* pend, const float* uend,
                 const float* wend, int on_device, cudaStream_t st) {
+  if (e->ckpt_k) return fail(SWIT_E_STATE, "this call needs boundary saving (checkpoint_every = 0)");
   Grid<R> g = make_grid<R>(e);
   const size_t NB = (size_t)e->ns * e->nt * e->SL, NI = (size_t)e->ns * e->nx * e->nz;
   const bool in_b = e->variant == 2 && (e->nt - 2) % 2 == 0;
@@ -1207,6 +1299,18 @@ int swit_create(const swit_desc* d, swit_engine** out) {
     }
   }
   e->IL = e->variant >= 3 ? e->L : 0;
+  if (d->checkpoint_every < 0) {
+    delete e;
+    return fail(SWIT_E_ARG, "checkpoint_every must be >= 0 (got %d)", d->checkpoint_every);
+  }
+  if (d->checkpoint_every > 0 && e->variant != 3 && e->variant != 6) {
+    delete e;
+    return fail(SWIT_E_ARG, "checkpointed recomputation needs the vec or band kernels (kernel_variant 0, 3 or 6)");
+  }
+  e->ckpt_k = std::min(d->checkpoint_every, e->nt);
+  e->ckpt_m = e->ckpt_k ? (e->nt + e->ckpt_k - 1) / e->ckpt_k : 0;
+  e->snt = e->ckpt_k ? e->ckpt_k : e->nt;
+  e->sit0 = 1;
 #ifdef SWIT_NO_PDL
   e->pdl = false;
 #else
@@ -1323,7 +1427,8 @@ int swit_create(const swit_desc* d, swit_engine** out) {
     void** i2[] = {&e->pe2, &e->ue2, &e->we2};
     for (void** f : i2) AL(valloc(e, f, (size_t)ns * FSI));
   }
-  AL(valloc(e, &e->strips, (size_t)ns * e->nt * e->SL));
+  AL(valloc(e, &e->strips, (size_t)ns * e->snt * e->SL));
+  if (e->ckpt_k) AL(valloc(e, &e->ckpt, (size_t)e->ckpt_m * 3 * ns * FSZ));
   AL(valloc(e, &e->src, (size_t)ns * (e->nt + 1)));
   AL(valloc(e, &e->seis_t, (size_t)ns * e->nt * ngm));
   AL(valloc(e, &e->adj_t, (size_t)ns * e->nt * ngm));
@@ -1367,7 +1472,7 @@ int swit_create(const swit_desc* d, swit_engine** out) {
   // strips of step 1 that the reconstruction inserts at it = 2.
   cudaError_t ce = cudaMemset(e->seis_t, 0, (size_t)ns * e->nt * ngm * e->esz);
   if (ce == cudaSuccess) ce = cudaMemset(e->d_err, 0, sizeof(int));
-  if (ce == cudaSuccess) ce = cudaMemset(e->strips, 0, (size_t)ns * e->nt * e->SL * e->esz);
+  if (ce == cudaSuccess) ce = cudaMemset(e->strips, 0, (size_t)ns * e->snt * e->SL * e->esz);
   if (ce == cudaSuccess) ce = cudaMemset(e->adj_t, 0, (size_t)ns * e->nt * ngm * e->esz);
   if (ce == cudaSuccess) ce = cudaStreamCreateWithFlags(&e->cap, cudaStreamNonBlocking);
   if (ce != cudaSuccess) {
@@ -1381,7 +1486,7 @@ int swit_create(const swit_desc* d, swit_engine** out) {
   const int per_step = e->variant == 2 ? 1 : 2;
   const int fwaves = e->path == 1 ? ns : (ns + fwd_batch(e) - 1) / fwd_batch(e);
   e->launches_fwd = (e->variant == 4 || e->variant == 5) ? fwaves : per * (e->nt - 1) * per_step;
-  e->launches_bwd = e->variant == 4 ? per : per * (e->nt - 1) * per_step;
+  e->launches_bwd = e->variant == 4 ? per : per * (e->nt - 1) * per_step * (e->ckpt_k ? 2 : 1);
   *out = e;
   return 0;
 }

@@ -27,6 +27,7 @@ namespace swit {
 template <class R>
 struct Grid {
   int nx, nz, L, NX, NZ, LD, LDI, fs, fs_flag, nt, ngmax, SL;
+  int snt, sit0;  // strip steps held per shot and the step of slot 0: step it at (s * snt + it - sit0) * SL
   size_t FSZ;  // floats per PML field of one shot (NX * LD)
   size_t FSI;  // floats per interior field of one shot (nx * LDI)
   int IL;      // interior layout offset: interior (jz, jx) at ((jx-1+IL)*LDI + jz-1+IL); npml or 0
@@ -202,7 +203,7 @@ __global__ void __launch_bounds__(256) k_fwd_uw(Grid<R> g, Receivers rec, const 
   }
   // boundary strips of step it, fdcore.f90:130-159
   if (strips) {
-    R* b = strips + ((size_t)s * g.nt + (it - 1)) * g.SL;
+    R* b = strips + ((size_t)s * g.snt + (it - g.sit0)) * g.SL;
     const StripOff o = strip_offsets(g.nx, g.nz);
     const int jx = ix - L, jz = iz - L;
     if (jx >= 1 && jx <= g.nx) {
@@ -288,7 +289,7 @@ __global__ void __launch_bounds__(256) k_bwd_uw(Grid<R> g, const R* __restrict__
     const R alpha = g.B[k];
     we[ki] = we[ki] + alpha * (g.c1 * (pe[ki + 1] - pe[ki]) + g.c2 * (pe[ki + 2] - pe[ki - 1]));
   }
-  const R* b = strips + ((size_t)s * g.nt + (it - 2)) * g.SL;  // boundary(:, it-1)
+  const R* b = strips + ((size_t)s * g.snt + (it - 1 - g.sit0)) * g.SL;  // boundary(:, it-1)
   const StripOff o = strip_offsets(nx, nz);
   if (jz == nz - 1) we[ki] = b[o.B2 + jx - 1];
   if (jx == 1) ue[ki] = b[o.S2 + jz - 1];
@@ -355,7 +356,7 @@ __global__ void __launch_bounds__(256) k_bwd_p(Grid<R> g, Receivers rec, Sources
     pf = pf + alpha * (g.c1 * (ue[ki] - ue[ki - LDI] + we[ki] - we[ki - 1]) +
                        g.c2 * (ue[ki + LDI] - ue[ki - 2 * LDI] + we[ki + 1] - we[ki - 2]));
   }
-  const R* b = strips + ((size_t)s * g.nt + (it - 2)) * g.SL;
+  const R* b = strips + ((size_t)s * g.snt + (it - 1 - g.sit0)) * g.SL;
   const StripOff o = strip_offsets(nx, nz);
   // re-insert in the reference's order: bottom, sides, top (last write wins)
   if (jz == nz) pf = b[o.B0 + jx - 1];

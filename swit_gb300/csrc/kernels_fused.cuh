@@ -85,7 +85,7 @@ __global__ void __launch_bounds__(1024) k_fwd_step(Grid<R> g, Sources src, Recei
   const bool w_row = iz >= fs && iz <= NZ - 2;
   const int isx = src.isx[s], isz = src.isz[s];
   const R sval = dt * s_fwd[(size_t)s * (g.nt + 1) + (it - 1)];
-  R* b = strips ? strips + ((size_t)s * g.nt + (it - 1)) * g.SL : nullptr;
+  R* b = strips ? strips + ((size_t)s * g.snt + (it - g.sit0)) * g.SL : nullptr;
   const StripOff so = strip_offsets(g.nx, g.nz);
   const int* cp = rec.colptr + (size_t)s * (NX + 2);
   R* trace = seis_t + ((size_t)s * g.nt + (it - 1)) * g.ngmax;
@@ -238,7 +238,7 @@ __global__ void __launch_bounds__(1024) k_bwd_step(
   const bool ue_row = jz >= fsi + 1 && jz <= nz - 1;
   const bool we_row = jz >= fsi + 1 && jz <= nz - 2;
   const bool pe_row = jz >= fsi + 2 && jz <= nz - 2;
-  const R* b = strips + ((size_t)s * g.nt + (it - 2)) * g.SL;  // boundary(:, it-1)
+  const R* b = strips + ((size_t)s * g.snt + (it - 1 - g.sit0)) * g.SL;  // boundary(:, it-1)
   const StripOff so = strip_offsets(nx, nz);
   const int* cp = rec.colptr + (size_t)s * (NX + 2);
   const R* adj = adj_t + ((size_t)s * g.nt + (it - 1)) * g.ngmax;

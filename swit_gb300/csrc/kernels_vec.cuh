@@ -359,7 +359,7 @@ __device__ __forceinline__ void fwd_uw_body(const Grid<R>& g, const Receivers& r
   const bool strip_rows = (iz0 <= fs + 2 && iz0 + 3 >= fs) || (iz0 <= NZ - L && iz0 + 3 >= NZ - L - 1);
   const bool strip_cols = ix == L + 1 || ix == L + 2 || ix == NX - L || ix == NX - L - 1;
   if (strips && (strip_rows || strip_cols)) {
-    R* bs = strips + ((size_t)v.s * g.nt + (it - 1)) * g.SL;
+    R* bs = strips + ((size_t)v.s * g.snt + (it - g.sit0)) * g.SL;
     const StripOff o = strip_offsets(g.nx, g.nz);
     const int jx = ix - L;
 #pragma unroll
@@ -497,7 +497,7 @@ __device__ __forceinline__ void bwd_uw_body(const Grid<R>& g, const R* __restric
     }
   }
   if (CHK) {
-    const R* b = strips + ((size_t)v.s * g.nt + (it - 2)) * g.SL;  // boundary(:, it-1)
+    const R* b = strips + ((size_t)v.s * g.snt + (it - 1 - g.sit0)) * g.SL;  // boundary(:, it-1)
     const StripOff o = strip_offsets(nx, nz);
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
@@ -612,7 +612,7 @@ __device__ __forceinline__ void bwd_p_body(const Grid<R>& g, const Receivers& re
     }
   }
   V4<R> g0 = ld4(dg, v.kg), f0 = ld4(dfw, v.kg), k0 = ld4(dbk, v.kg);
-  const R* b = CHK ? strips + ((size_t)v.s * g.nt + (it - 2)) * g.SL : nullptr;
+  const R* b = CHK ? strips + ((size_t)v.s * g.snt + (it - 1 - g.sit0)) * g.SL : nullptr;
   const StripOff o = strip_offsets(nx, nz);
 #pragma unroll
   for (int j = 0; j < 4; ++j) {

@@ -263,6 +263,8 @@ extern "C" int swit_forward_shot_static(int32_t nx, int32_t nz, int32_t npml, in
   g.nt = nt;
   g.ngmax = ng;
   g.SL = 0;
+  g.snt = nt;
+  g.sit0 = 1;
   g.FSZ = 0;  // one shot
   g.FSI = 0;
   g.IL = 0;

@@ -27,7 +27,7 @@ class Engine:
     """
 
     def __init__(self, nx, nz, npml, nt, dx, dt, src_xz, rec_xz, free_surface=1, ng=None, precision="fp32",
-                 path="batched", shots_per_batch=0, block_x=0, kernel="auto"):
+                 path="batched", shots_per_batch=0, block_x=0, kernel="auto", checkpoint_every=0):
         lib = _lib.load()
         src_xz = np.asarray(src_xz, dtype=np.float32).reshape(-1, 2)
         rec_xz = np.asarray(rec_xz, dtype=np.float32)
@@ -56,7 +56,9 @@ class Engine:
         d = _lib.SwitDesc(self.nx, self.nz, self.npml, self.nt, self.dx, self.dt, int(free_surface), self.ns,
                           self.ngmax, k["ng"].ctypes.data, k["xs"].ctypes.data, k["zs"].ctypes.data,
                           k["xg"].ctypes.data, k["zg"].ctypes.data, 1 if self.fp64 else 0,
-                          1 if path == "plain" else 0, int(shots_per_batch), int(block_x), variants[kernel])
+                          1 if path == "plain" else 0, int(shots_per_batch), int(block_x), variants[kernel],
+                          int(checkpoint_every))
+        self.checkpoint_every = int(checkpoint_every)
         h = C.c_void_p()
         _lib.check(lib.swit_create(C.byref(d), C.byref(h)))
         self._h = h
@@ -217,6 +219,27 @@ class Engine:
 
     def __exit__(self, *a):
         self.close()
+
+
+def checkpoint_interval(nx, nz, npml, nt, ns, budget_bytes, fp64=False):
+    """Memory strategy for a survey: 0 (boundary saving, fd2dmpi's own) when the
+    strips of all shots fit in ``budget_bytes`` together with the wavefields,
+    else the checkpoint interval k that minimises checkpoints + strip buffer,
+    ns * (ceil((nt-1)/k) * 3 * NX * LD + k * (9 nx + 6 nz)) values (the
+    allocation of swit_create with checkpoint_every = k)."""
+    esz = 8 if fp64 else 4
+    NX, NZ = nx + 2 * npml, nz + 2 * npml
+    fsz = NX * ((NZ + 31) // 32) * 32
+    sl = 9 * nx + 6 * nz
+    fields = 12 * ns * fsz * esz
+    if ns * nt * sl * esz + fields <= budget_bytes:
+        return 0
+
+    def mem(k):
+        return ns * (-(-(nt - 1) // k) * 3 * fsz + k * sl) * esz
+
+    k0 = max(1, int(round(((nt - 1) * 3 * fsz / sl) ** 0.5)))
+    return min(range(max(1, k0 // 2), min(nt, 2 * k0) + 1), key=mem)
 
 
 def damp_profile(nx, nz, npml, dx, vmin):

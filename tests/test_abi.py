@@ -46,7 +46,8 @@ def _desc(s, **over):
     (dict(nx=4), _lib.SwitError), (dict(npml=1), _lib.SwitError), (dict(nt=1), _lib.SwitError),
     (dict(dx=0.0), _lib.SwitError), (dict(precision=3), _lib.SwitError),
     (dict(block_x=3, kernel_variant=1), _lib.SwitError), (dict(block_x=12, kernel_variant=2), _lib.SwitError),
-    (dict(kernel_variant=7), _lib.SwitError),
+    (dict(kernel_variant=7), _lib.SwitError), (dict(checkpoint_every=-1), _lib.SwitError),
+    (dict(checkpoint_every=5, kernel_variant=1), _lib.SwitError),
 ])
 def test_create_rejects_bad_descriptions_before_any_gpu_work(over, code):
     lib = _lib.load()
