@@ -46,6 +46,11 @@ def parse():
     ap.add_argument("--kernel", default="auto", choices=["auto", "fused", "split", "vec", "cluster", "hybrid", "band"])
     ap.add_argument("--no-tune", action="store_true", help="skip the launch-configuration autotuner")
     ap.add_argument("--no-extras", action="store_true", help="skip plain path, CPU baseline and kernel profile")
+    ap.add_argument("--workload", default="marmousi", choices=["marmousi", "large"],
+                    help="marmousi: 481x141 nt 4000 49 shots (the headline); large: 2001x601 nt 6000 200 shots")
+    ap.add_argument("--checkpoint", default="0",
+                    help="memory strategy: 0 = boundary saving, k = checkpoints every k steps, auto = the interval "
+                         "that minimises memory")
     return ap.parse_args()
 
 
@@ -223,15 +228,21 @@ def run_mine(args):
     torch.cuda.set_device(local)
     if world > 1:
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
-    per_rank = args.shots or 49
-    full = survey.config(1, ns=per_rank * world, nt=args.nt)
+    large = args.workload == "large"
+    if large:  # no autotune (each trial engine would hold the full survey) and no CPU-side extras
+        args.no_tune = args.no_extras = True
+    per_rank = args.shots or (200 if large else 49)
+    full = survey.config(3 if large else 1, ns=per_rank * world, nt=args.nt)
     # rank r owns a contiguous block of shots (fd2dmpi/mmi_mpi.f90:52-80)
     lo, hi = shots.assigned(per_rank * world, rank, world)
     sv = full
     src_xz, rec_xz = full.src_xz[lo:hi], full.rec_xz[lo:hi]
     rho = sv.rho(sv.vp_true)
     src = sv.source()[lo:hi].copy()
-    opts = dict(shots_per_batch=args.batch, block_x=args.block_x, kernel=args.kernel)
+    from swit_gb300.engine import checkpoint_interval
+    ckpt = (checkpoint_interval(sv.nx, sv.nz, sv.npml, sv.nt, per_rank, 0) if args.checkpoint == "auto"
+            else int(args.checkpoint))
+    opts = dict(shots_per_batch=args.batch, block_x=args.block_x, kernel=args.kernel, checkpoint_every=ckpt)
     tuned = None
     if not args.no_tune and args.batch == 0 and args.block_x == 0 and args.kernel == "auto":
         from swit_gb300 import autotune
@@ -266,7 +277,7 @@ def run_mine(args):
     torch.cuda.synchronize()
     ev0.record(stream)
     for _ in range(args.steps):
-        step_device()
+        last = step_device()
     ev1.record(stream)
     torch.cuda.synchronize()
     clk = clocks.stop()
@@ -334,6 +345,13 @@ def run_mine(args):
                     "d2h_bytes_per_step": int(d2h)},
             "clocks": clk,
             "gpu_launches": int(args.steps * (q["kernels_per_forward"] + q["kernels_per_backward"] + 5))}
+    import hashlib
+    gh = last["grad"].detach().float().cpu().numpy()
+    line["config"]["memory"] = {
+        "strategy": "checkpoints every %d steps" % ckpt if ckpt else "boundary saving",
+        "device_bytes": q["device_bytes"],
+        "gradient_sha256": hashlib.sha256(gh.tobytes()).hexdigest()[:16],
+        "gradient_l2": float(np.linalg.norm(gh.astype(np.float64)))}
 
     if not args.no_extras:
         # per-kernel launch durations (CUDA events around every launch)

@@ -221,22 +221,24 @@ class Engine:
         self.close()
 
 
-def checkpoint_interval(nx, nz, npml, nt, ns, budget_bytes, fp64=False):
+def checkpoint_interval(nx, nz, npml, nt, ns, budget_bytes, ng=None, fp64=False):
     """Memory strategy for a survey: 0 (boundary saving, fd2dmpi's own) when the
-    strips of all shots fit in ``budget_bytes`` together with the wavefields,
+    engine with the strips of all shots fits in ``budget_bytes`` (wavefields,
+    imaging sums and trace staging included; ng receivers per shot, default nx),
     else the checkpoint interval k that minimises checkpoints + strip buffer,
-    ns * (ceil((nt-1)/k) * 3 * NX * LD + k * (9 nx + 6 nz)) values (the
-    allocation of swit_create with checkpoint_every = k)."""
+    ns * (ceil(nt/k) * 3 * NX * LD + k * (9 nx + 6 nz)) values (the allocation of
+    swit_create with checkpoint_every = k)."""
     esz = 8 if fp64 else 4
     NX, NZ = nx + 2 * npml, nz + 2 * npml
     fsz = NX * ((NZ + 31) // 32) * 32
     sl = 9 * nx + 6 * nz
-    fields = 12 * ns * fsz * esz
-    if ns * nt * sl * esz + fields <= budget_bytes:
+    ng = nx if ng is None else ng
+    rest = 12 * ns * fsz * esz + ns * ng * nt * (3 * esz + 4)  # fields and sums; seis, adjoint, staging, input
+    if ns * nt * sl * esz + rest <= budget_bytes:
         return 0
 
     def mem(k):
-        return ns * (-(-(nt - 1) // k) * 3 * fsz + k * sl) * esz
+        return ns * (-(-nt // k) * 3 * fsz + k * sl) * esz
 
     k0 = max(1, int(round(((nt - 1) * 3 * fsz / sl) ** 0.5)))
     return min(range(max(1, k0 // 2), min(nt, 2 * k0) + 1), key=mem)

@@ -131,6 +131,23 @@ def faulted_layers(nx=481, nz=141, dx=25.0, seed=1001, nlayers=30, vmin=1500.0, 
     return np.clip(vp, vmin, vmax * (1 + noise)).astype(np.float32)
 
 
+def smooth_layered_random(nx=2001, nz=601, dx=10.0, seed=1003, vmin=1500.0, vmax=5000.0, nlayers=12,
+                          corr_m=200.0, std=0.04):
+    """Smooth-plus-layered model vmin..vmax with a 2-D Gaussian-correlated random field (relative std, correlation
+    length corr_m), clipped to [vmin, 1.1 vmax]."""
+    rng = np.random.default_rng(seed)
+    z = np.arange(nz) * dx
+    trend = vmin + (vmax - vmin) * (z / z[-1]) ** 0.8
+    steps = np.sort(rng.uniform(0.1, 0.95, nlayers)) * z[-1]
+    jumps = rng.uniform(-150.0, 250.0, nlayers)
+    layered = trend + sum(j * (z > s0) for j, s0 in zip(jumps, steps))
+    vp = np.broadcast_to(layered, (nx, nz)).astype(np.float64)
+    field = gaussian_filter(rng.standard_normal((nx, nz)), sigma=corr_m / dx / np.sqrt(2.0), mode="wrap")
+    field /= field.std()
+    vp = vp * (1.0 + std * field)
+    return np.clip(vp, vmin, 1.1 * vmax).astype(np.float32)
+
+
 def smooth(vp, sigma_m, dx, keep_top=0):
     out = gaussian_filter(np.asarray(vp, np.float64), sigma=sigma_m / dx, mode="nearest")
     if keep_top:
@@ -139,7 +156,8 @@ def smooth(vp, sigma_m, dx, keep_top=0):
 
 
 def config(idx, ns=None, nt=None):
-    """The seeded survey of benchmark configuration idx (0: plain small, 1: batched Marmousi-like)."""
+    """The seeded survey of benchmark configuration idx (0: plain small, 1: batched Marmousi-like,
+    3: large memory-bound case)."""
     if idx == 0:
         nx, nz, dx, dt, nt_, npml, f0 = 201, 101, 25.0, 0.002, 2000, 40, 5.0
         vp = layered_anomaly(nx, nz, dx, seed=1000)
@@ -152,6 +170,12 @@ def config(idx, ns=None, nt=None):
         init = smooth(vp, 250.0, dx, keep_top=12)
         src, rec = _line_geometry(nx, dx, 49 if ns is None else ns, 25.0, 25.0)
         name = "marmousi-like 481x141 dx25 nt4000 49 shots"
+    elif idx == 3:
+        nx, nz, dx, dt, nt_, npml, f0 = 2001, 601, 10.0, 0.001, 6000, 60, 10.0
+        vp = smooth_layered_random(nx, nz, dx, seed=1003)
+        init = smooth(vp, 200.0, dx)
+        src, rec = _line_geometry(nx, dx, 200 if ns is None else ns, 20.0, 20.0)
+        name = "large 2001x601 dx10 nt6000 200 shots"
     else:
         raise ValueError("configuration %d is not generated here" % idx)
     return Survey(name=name, nx=nx, nz=nz, dx=dx, dt=dt, nt=nt_ if nt is None else nt, npml=npml, f0=f0,
