@@ -211,6 +211,37 @@ int swit_query(const swit_engine* e, int64_t* device_bytes, int32_t* shots_per_b
  * reference, whose CPU loops have no asynchronous copies. */
 int swit_check(swit_engine* e, void* stream);
 
+/* ---- Many independent problems in one set of launches --------------------
+ * A multi-instance engine holds n regular engines (one swit_desc each: FP32,
+ * batched path, vec kernels, boundary saving; grids, shot counts and nt may all
+ * differ) and steps all of them together: each time step launches the four
+ * phase kernels once over every instance still running.  The reference runs one
+ * fd2dmpi job per problem; this has no counterpart there.  Models are set per
+ * instance through the handles of swit_multi_engine, which stay owned by the
+ * multi-instance engine. */
+typedef struct swit_multi swit_multi;
+
+int swit_multi_create(const swit_desc* descs, int32_t n, swit_multi** out);
+
+/* Borrowed handle of instance i (caller order) for swit_set_model, swit_query,
+ * or single-instance calls. */
+int swit_multi_engine(swit_multi* m, int32_t i, swit_engine** e);
+
+/* swit_gradient_l2 for every instance: src[i] (ns_i, nt_i), obs[i]
+ * (ns_i, ng_max_i, nt_i) float; grad[i], illum_fw[i], illum_bk[i] (nx_i, nz_i),
+ * any array or entry may be NULL; misfit[i] on the host (waits), or misfit
+ * NULL.  Every instance gets the bits its own engine's swit_gradient_l2 gives. */
+int swit_multi_gradient_l2(swit_multi* m, const float* const* src, const float* const* obs, void* const* grad,
+                           void* const* illum_fw, void* const* illum_bk, double* misfit, int32_t on_device,
+                           void* stream);
+
+/* Waveform misfit of every instance (forward runs only, no strips); misfit[n]
+ * on the host (waits). */
+int swit_multi_misfit_l2(swit_multi* m, const float* const* src, const float* const* obs, double* misfit,
+                         int32_t on_device, void* stream);
+
+int swit_multi_destroy(swit_multi* m);
+
 /* Releases the engine and its device memory. */
 int swit_destroy(swit_engine* e);
 

@@ -21,6 +21,7 @@
 #include "kernels_vec.cuh"
 #include "kernels_cluster.cuh"
 #include "kernels_band.cuh"
+#include "kernels_multi.cuh"
 
 using namespace swit;
 
@@ -70,6 +71,7 @@ struct swit_engine {
   uint32_t* d_list = nullptr;
   size_t list_stride = 0;
   int list_n0[4] = {0, 0, 0, 0}, list_n1[4] = {0, 0, 0, 0}, list_len[4] = {0, 0, 0, 0};
+  std::vector<uint32_t> h_list;  // host copy of the four lists (multi-instance engines combine them)
   // band variant: columns per band, bands, per-band task lists and counts of the four kernels
   int band_bc = 0, nbands = 0, band_stride = 0;
   uint32_t* d_blist = nullptr;
@@ -604,7 +606,8 @@ int stage_input(swit_engine* e, const float* in, size_t n, int on_device, cudaSt
 }
 
 template <class R>
-int forward_impl(swit_engine* e, const float* src, void* seis, bool store, int on_device, cudaStream_t st) {
+int forward_impl(swit_engine* e, const float* src, void* seis, bool store, int on_device, cudaStream_t st,
+                 bool run_loop = true) {
   Grid<R> g = make_grid<R>(e);
   const float* dsrc;
   int rc = stage_input(e, src, (size_t)e->ns * e->nt, on_device, st, &dsrc);
@@ -619,8 +622,10 @@ int forward_impl(swit_engine* e, const float* src, void* seis, bool store, int o
     CK(cudaMemsetAsync(e->u2, 0, fb, st));
     CK(cudaMemsetAsync(e->w2, 0, fb, st));
   }
-  rc = run_forward_loop<R>(e, store, st);
-  if (rc) return rc;
+  if (run_loop) {  // a multi-instance engine runs the loops of all its instances itself
+    rc = run_forward_loop<R>(e, store, st);
+    if (rc) return rc;
+  }
   if (seis) {
     dim3 grid((e->nt + 31) / 32, (e->ngmax + 31) / 32, e->ns), block(32, 8);
     void* out = on_device ? seis : e->d_stage;
@@ -633,6 +638,25 @@ int forward_impl(swit_engine* e, const float* src, void* seis, bool store, int o
   }
   CK(cudaGetLastError());
   e->fwd_ready = store;
+  return 0;
+}
+
+template <class R>
+int backward_end(swit_engine* e, void* grad, void* fw, void* bk, int on_device, cudaStream_t st);
+
+// Zeroed adjoint state and imaging sums, reconstruction start: everything of
+// the reverse job before its time loop (vec kernels).
+template <class R>
+int backward_begin(swit_engine* e, cudaStream_t st) {
+  Grid<R> g = make_grid<R>(e);
+  const size_t fb = (size_t)e->ns * g.FSZ * e->esz, ib = (size_t)e->ns * g.FSI * e->esz;
+  CK(cudaMemsetAsync(e->pb, 0, fb, st));
+  CK(cudaMemsetAsync(e->ub, 0, fb, st));
+  CK(cudaMemsetAsync(e->wb, 0, fb, st));
+  CK(cudaMemsetAsync(e->dg, 0, ib, st));
+  CK(cudaMemsetAsync(e->dfw, 0, ib, st));
+  CK(cudaMemsetAsync(e->dbk, 0, ib, st));
+  copy_end<R>(e, st);
   return 0;
 }
 
@@ -656,6 +680,13 @@ int backward_core(swit_engine* e, void* grad, void* fw, void* bk, int on_device,
   copy_end<R>(e, st);
   int rc = run_backward_loop<R>(e, st);
   if (rc) return rc;
+  return backward_end<R>(e, grad, fw, bk, on_device, st);
+}
+
+// Shot sum, scaling and outputs after the reverse loop (solver.f90:263-279).
+template <class R>
+int backward_end(swit_engine* e, void* grad, void* fw, void* bk, int on_device, cudaStream_t st) {
+  Grid<R> g = make_grid<R>(e);
   const size_t NI = (size_t)e->nx * e->nz;
   char* stage = (char*)e->d_stage;
   void* og = on_device ? grad : (grad ? stage : nullptr);
@@ -687,31 +718,43 @@ int backward_impl(swit_engine* e, const float* adj, void* grad, void* fw, void* 
   return backward_core<R>(e, grad, fw, bk, on_device, st);
 }
 
+// Waveform misfit per trace and its adjoint source syn - obs for live traces
+// (misfit.py:128-148, 263-282), from the synthetics of the last forward run.
 template <class R>
-int gradient_impl(swit_engine* e, const float* src, const float* obs, void* grad, void* fw, void* bk, void* seis,
-                  double* misfit, int on_device, cudaStream_t st) {
-  // the forward stages the source through d_in; obs needs its own staging
-  int rc = forward_impl<R>(e, src, seis, true, on_device, st);
-  if (rc) return rc;
+int residual_l2(swit_engine* e, const float* obs, int on_device, cudaStream_t st) {
   const float* dobs;
-  rc = stage_input(e, obs, (size_t)e->ns * e->ngmax * e->nt, on_device, st, &dobs);
+  int rc = stage_input(e, obs, (size_t)e->ns * e->ngmax * e->nt, on_device, st, &dobs);
   if (rc) return rc;
   k_trace_stats<R><<<dim3(e->ngmax, e->ns), 256, 0, st>>>((const R*)e->seis_t, dobs, e->d_ng, e->nt, e->ngmax,
                                                           e->dt32, e->d_live, e->d_mtrace);
   dim3 grid((e->nt + 31) / 32, (e->ngmax + 31) / 32, e->ns), block(32, 8);
   k_residual<R><<<grid, block, 0, st>>>((const R*)e->seis_t, dobs, e->d_live, (R*)e->adj_t, e->nt, e->ngmax);
   CK(cudaGetLastError());
+  return 0;
+}
+
+// Sum of the per-trace misfits on the host (waits for the stream).
+int misfit_sum(swit_engine* e, cudaStream_t st, double* misfit) {
+  std::vector<double> mt((size_t)e->ns * e->ngmax);
+  CK(cudaMemcpyAsync(mt.data(), e->d_mtrace, mt.size() * sizeof(double), cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  double acc = 0.0;
+  for (double v : mt) acc += v;
+  *misfit = acc;
+  return 0;
+}
+
+template <class R>
+int gradient_impl(swit_engine* e, const float* src, const float* obs, void* grad, void* fw, void* bk, void* seis,
+                  double* misfit, int on_device, cudaStream_t st) {
+  // the forward stages the source through d_in; obs needs its own staging
+  int rc = forward_impl<R>(e, src, seis, true, on_device, st);
+  if (rc) return rc;
+  rc = residual_l2<R>(e, obs, on_device, st);
+  if (rc) return rc;
   rc = backward_core<R>(e, grad, fw, bk, on_device, st);
   if (rc) return rc;
-  if (misfit) {
-    std::vector<double> mt((size_t)e->ns * e->ngmax);
-    CK(cudaMemcpyAsync(mt.data(), e->d_mtrace, mt.size() * sizeof(double), cudaMemcpyDeviceToHost, st));
-    CK(cudaStreamSynchronize(st));
-    double acc = 0.0;
-    for (double v : mt) acc += v;
-    *misfit = acc;
-  }
-  return 0;
+  return misfit ? misfit_sum(e, st, misfit) : 0;
 }
 
 // Model setup on the host, in R: padding (io.f90:231-300), vmin
@@ -1062,6 +1105,7 @@ int build_lists(swit_engine* e) {
     e->list_len[k] = m;
   }
   e->list_stride = n;
+  e->h_list = L;
   int rc = dalloc(e, &e->d_list, 4 * n);
   if (rc) return rc;
   CK(cudaMemcpy(e->d_list, L.data(), 4 * n * sizeof(uint32_t), cudaMemcpyHostToDevice));
@@ -1216,6 +1260,140 @@ int setup_cluster(swit_engine* e, int want) {
   if (rc == 0 && e->variant == 4)
     rc = e->maxt_b == 512 ? cluster_attrs<R, 512>(e, false, true) : cluster_attrs<R, 1024>(e, false, true);
   return rc;
+}
+
+}  // namespace
+
+// Many independent problems stepped together (kernels_multi.cuh).
+struct swit_multi {
+  std::vector<swit_engine*> eng;  // owned, caller order
+  std::vector<int> order;         // caller indices by record length, longest first (table and list order)
+  int max_nt = 0, max_ns = 0;
+  Inst<float>* d_tab = nullptr;
+  uint64_t* d_list[4] = {nullptr, nullptr, nullptr, nullptr};
+  std::vector<int> act[4];  // active prefix: [k][s] at forward step s (k = 0, 1) or reverse index s (k = 2, 3)
+  cudaStream_t cap = nullptr;
+  cudaGraphExec_t gf[2] = {nullptr, nullptr};
+  cudaGraphExec_t gb = nullptr;
+};
+
+namespace {
+
+void multi_release(swit_multi* m) {
+  for (int i = 0; i < 2; ++i)
+    if (m->gf[i]) cudaGraphExecDestroy(m->gf[i]);
+  if (m->gb) cudaGraphExecDestroy(m->gb);
+  if (m->cap) cudaStreamDestroy(m->cap);
+  if (m->d_tab) cudaFree(m->d_tab);
+  for (uint64_t* l : m->d_list)
+    if (l) cudaFree(l);
+  for (swit_engine* e : m->eng) {
+    release(e);
+    delete e;
+  }
+}
+
+// Combined task lists, active prefixes and the instance table.
+int multi_build(swit_multi* m) {
+  const int n = (int)m->eng.size();
+  m->order.resize(n);
+  for (int i = 0; i < n; ++i) m->order[i] = i;
+  std::stable_sort(m->order.begin(), m->order.end(), [&](int a, int b) { return m->eng[a]->nt > m->eng[b]->nt; });
+  m->max_nt = m->eng[m->order[0]]->nt;
+  std::vector<Inst<float>> tab(n);
+  for (int r = 0; r < n; ++r) {
+    swit_engine* e = m->eng[m->order[r]];
+    m->max_ns = std::max(m->max_ns, e->ns);
+    Inst<float>& I = tab[r];
+    I.g = make_grid<float>(e);
+    I.rec = make_rec(e);
+    I.src = make_src(e);
+    I.ns = e->ns;
+    I.s_fwd = (const float*)e->src;
+    I.p = (float*)e->p;
+    I.u = (float*)e->u;
+    I.w = (float*)e->w;
+    I.seis_t = (float*)e->seis_t;
+    I.strips = (float*)e->strips;
+    I.pb = (float*)e->pb;
+    I.ub = (float*)e->ub;
+    I.wb = (float*)e->wb;
+    I.pe = (float*)e->pe;
+    I.ue = (float*)e->ue;
+    I.we = (float*)e->we;
+    I.dg = (float*)e->dg;
+    I.dfw = (float*)e->dfw;
+    I.dbk = (float*)e->dbk;
+    I.adj_t = (const float*)e->adj_t;
+  }
+  CK(cudaMalloc(&m->d_tab, n * sizeof(Inst<float>)));
+  CK(cudaMemcpy(m->d_tab, tab.data(), n * sizeof(Inst<float>), cudaMemcpyHostToDevice));
+  for (int k = 0; k < 4; ++k) {
+    std::vector<uint64_t> L;
+    std::vector<int> cum(n);
+    for (int r = 0; r < n; ++r) {
+      const swit_engine* e = m->eng[m->order[r]];
+      const uint32_t* src = &e->h_list[(size_t)k * e->list_stride];
+      for (int i = 0; i < e->list_len[k]; ++i) {
+        const uint64_t t = i < e->list_n0[k] ? 0 : (i < e->list_n1[k] ? 1 : 2);
+        L.push_back(((uint64_t)r << 40) | (t << 32) | src[i]);
+      }
+      cum[r] = (int)L.size();
+    }
+    CK(cudaMalloc(&m->d_list[k], std::max<size_t>(L.size(), 1) * sizeof(uint64_t)));
+    CK(cudaMemcpy(m->d_list[k], L.data(), L.size() * sizeof(uint64_t), cudaMemcpyHostToDevice));
+    // instances with nt >= s run forward step s and reverse index s - 2: a prefix of the order
+    m->act[k].assign(m->max_nt + 1, 0);
+    for (int s = 2; s <= m->max_nt; ++s) {
+      int nr = 0;
+      while (nr < n && m->eng[m->order[nr]]->nt >= s) ++nr;
+      const int a = nr ? cum[nr - 1] : 0;
+      if (k < 2)
+        m->act[k][s] = a;
+      else
+        m->act[k][s - 2] = a;
+    }
+  }
+  CK(cudaStreamCreateWithFlags(&m->cap, cudaStreamNonBlocking));
+  return 0;
+}
+
+// The forward (which = 0: no strips, 1: with strips) or reverse (which = 2)
+// loop of every instance, one launch per phase and step, captured once.
+int multi_loop(swit_multi* m, int which, cudaStream_t st) {
+  cudaGraphExec_t& ex = which == 2 ? m->gb : m->gf[which];
+  if (!ex) {
+    cudaGraph_t graph;
+    CK(cudaStreamBeginCapture(m->cap, cudaStreamCaptureModeThreadLocal));
+    const dim3 block(256);
+    auto grid = [&](int len) { return dim3((unsigned)std::max(1, (len + 255) / 256), (unsigned)m->max_ns); };
+    const Inst<float>* tab = m->d_tab;
+    if (which < 2) {
+      for (int it = 2; it <= m->max_nt; ++it) {
+        launch_pdl(true, k_fwd_p_m<float>, grid(m->act[0][it]), block, m->cap, tab, (const uint64_t*)m->d_list[0],
+                   m->act[0][it], it);
+        launch_pdl(true, k_fwd_uw_m<float>, grid(m->act[1][it]), block, m->cap, tab, (const uint64_t*)m->d_list[1],
+                   m->act[1][it], it, which);
+      }
+    } else {
+      for (int jr = 0; jr <= m->max_nt - 2; ++jr) {
+        launch_pdl(true, k_bwd_uw_m<float>, grid(m->act[2][jr]), block, m->cap, tab, (const uint64_t*)m->d_list[2],
+                   m->act[2][jr], jr);
+        launch_pdl(true, k_bwd_p_m<float>, grid(m->act[3][jr]), block, m->cap, tab, (const uint64_t*)m->d_list[3],
+                   m->act[3][jr], jr);
+      }
+    }
+    cudaError_t rc = cudaStreamEndCapture(m->cap, &graph);
+    if (rc != cudaSuccess) return fail(SWIT_E_CUDA, "multi-instance graph capture: %s", cudaGetErrorString(rc));
+    rc = cudaGraphInstantiate(&ex, graph, 0);
+    cudaGraphDestroy(graph);
+    if (rc != cudaSuccess) {
+      ex = nullptr;
+      return fail(SWIT_E_CUDA, "multi-instance graph instantiate: %s", cudaGetErrorString(rc));
+    }
+  }
+  CK(cudaGraphLaunch(ex, st));
+  return 0;
 }
 
 }  // namespace
@@ -1589,6 +1767,102 @@ int swit_check(swit_engine* e, void* stream) {
     CK(cudaMemset(e->d_err, 0, sizeof(int)));
     return fail(SWIT_E_TIMEOUT, "a kernel gave up waiting for its staged copies (error word %d); results are invalid", w);
   }
+  return 0;
+}
+
+int swit_multi_create(const swit_desc* descs, int32_t n, swit_multi** out) {
+  if (!descs || !out || n < 1) return fail(SWIT_E_ARG, "null argument or no instance");
+  if (n > 65535) return fail(SWIT_E_LIMIT, "at most 65535 instances");
+  *out = nullptr;
+  for (int i = 0; i < n; ++i) {
+    const swit_desc& d = descs[i];
+    if (d.precision != 0 || d.path != 0 || (d.kernel_variant != 0 && d.kernel_variant != 3) || d.checkpoint_every)
+      return fail(SWIT_E_ARG,
+                  "instance %d: a multi-instance engine runs FP32 vec kernels on the batched path with boundary saving",
+                  i);
+  }
+  swit_multi* m = new swit_multi();
+  for (int i = 0; i < n; ++i) {
+    swit_engine* e = nullptr;
+    int rc = swit_create(&descs[i], &e);
+    if (rc) {
+      std::string msg = g_err;
+      multi_release(m);
+      delete m;
+      return fail(rc, "instance %d: %s", i, msg.c_str());
+    }
+    m->eng.push_back(e);
+  }
+  int rc = multi_build(m);
+  if (rc) {
+    multi_release(m);
+    delete m;
+    return rc;
+  }
+  *out = m;
+  return 0;
+}
+
+int swit_multi_engine(swit_multi* m, int32_t i, swit_engine** e) {
+  if (!m || !e || i < 0 || i >= (int32_t)m->eng.size()) return fail(SWIT_E_ARG, "bad multi-instance handle or index");
+  *e = m->eng[i];
+  return 0;
+}
+
+int swit_multi_gradient_l2(swit_multi* m, const float* const* src, const float* const* obs, void* const* grad,
+                           void* const* illum_fw, void* const* illum_bk, double* misfit, int32_t on_device,
+                           void* stream) {
+  if (!m || !src || !obs) return fail(SWIT_E_ARG, "null argument");
+  cudaStream_t st = (cudaStream_t)stream;
+  const int n = (int)m->eng.size();
+  for (int i = 0; i < n; ++i)
+    if (!m->eng[i]->model_set) return fail(SWIT_E_STATE, "instance %d: swit_set_model has not been called", i);
+  for (int i = 0; i < n; ++i) {
+    int rc = forward_impl<float>(m->eng[i], src[i], nullptr, true, on_device, st, false);
+    if (rc) return rc;
+  }
+  int rc = multi_loop(m, 1, st);
+  if (rc) return rc;
+  for (int i = 0; i < n; ++i) {
+    if ((rc = residual_l2<float>(m->eng[i], obs[i], on_device, st))) return rc;
+    if ((rc = backward_begin<float>(m->eng[i], st))) return rc;
+  }
+  if ((rc = multi_loop(m, 2, st))) return rc;
+  for (int i = 0; i < n; ++i) {
+    rc = backward_end<float>(m->eng[i], grad ? grad[i] : nullptr, illum_fw ? illum_fw[i] : nullptr,
+                             illum_bk ? illum_bk[i] : nullptr, on_device, st);
+    if (rc) return rc;
+  }
+  if (misfit)
+    for (int i = 0; i < n; ++i)
+      if ((rc = misfit_sum(m->eng[i], st, &misfit[i]))) return rc;
+  return 0;
+}
+
+int swit_multi_misfit_l2(swit_multi* m, const float* const* src, const float* const* obs, double* misfit,
+                         int32_t on_device, void* stream) {
+  if (!m || !src || !obs || !misfit) return fail(SWIT_E_ARG, "null argument");
+  cudaStream_t st = (cudaStream_t)stream;
+  const int n = (int)m->eng.size();
+  for (int i = 0; i < n; ++i)
+    if (!m->eng[i]->model_set) return fail(SWIT_E_STATE, "instance %d: swit_set_model has not been called", i);
+  for (int i = 0; i < n; ++i) {
+    int rc = forward_impl<float>(m->eng[i], src[i], nullptr, false, on_device, st, false);
+    if (rc) return rc;
+  }
+  int rc = multi_loop(m, 0, st);
+  if (rc) return rc;
+  for (int i = 0; i < n; ++i)
+    if ((rc = residual_l2<float>(m->eng[i], obs[i], on_device, st))) return rc;
+  for (int i = 0; i < n; ++i)
+    if ((rc = misfit_sum(m->eng[i], st, &misfit[i]))) return rc;
+  return 0;
+}
+
+int swit_multi_destroy(swit_multi* m) {
+  if (!m) return 0;
+  multi_release(m);
+  delete m;
   return 0;
 }
 

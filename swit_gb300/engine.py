@@ -27,7 +27,7 @@ class Engine:
     """
 
     def __init__(self, nx, nz, npml, nt, dx, dt, src_xz, rec_xz, free_surface=1, ng=None, precision="fp32",
-                 path="batched", shots_per_batch=0, block_x=0, kernel="auto", checkpoint_every=0):
+                 path="batched", shots_per_batch=0, block_x=0, kernel="auto", checkpoint_every=0, _borrow=None):
         lib = _lib.load()
         src_xz = np.asarray(src_xz, dtype=np.float32).reshape(-1, 2)
         rec_xz = np.asarray(rec_xz, dtype=np.float32)
@@ -59,10 +59,15 @@ class Engine:
                           1 if path == "plain" else 0, int(shots_per_batch), int(block_x), variants[kernel],
                           int(checkpoint_every))
         self.checkpoint_every = int(checkpoint_every)
+        self._desc = d
+        self._lib = lib
+        self._owned = _borrow is None
+        if _borrow is not None:  # an instance of a MultiEngine, which owns the handle
+            self._h = _borrow
+            return
         h = C.c_void_p()
         _lib.check(lib.swit_create(C.byref(d), C.byref(h)))
         self._h = h
-        self._lib = lib
 
     # ------------------------------------------------------------------ utils
     @property
@@ -205,7 +210,8 @@ class Engine:
 
     def close(self):
         if getattr(self, "_h", None):
-            self._lib.swit_destroy(self._h)
+            if getattr(self, "_owned", True):
+                self._lib.swit_destroy(self._h)
             self._h = None
 
     def __del__(self):
@@ -218,6 +224,91 @@ class Engine:
         return self
 
     def __exit__(self, *a):
+        self.close()
+
+
+class MultiEngine:
+    """Many independent problems (grids, shot counts, record lengths may all
+    differ) stepped together: each time step launches the four phase kernels
+    once over every problem still running (swit_multi_*).  ``problems`` is a list
+    of Engine keyword dicts (nx, nz, npml, nt, dx, dt, src_xz, rec_xz[, ng,
+    free_surface, block_x]); ``engines[i]`` is problem i's Engine (set_model,
+    forward, ... work on it alone)."""
+
+    def __init__(self, problems):
+        lib = _lib.load()
+        views = [Engine(**p, _borrow=C.c_void_p(1)) for p in problems]  # descriptions only
+        for v in views:
+            if v.fp64 or v.path != "batched" or v.checkpoint_every:
+                raise ValueError("a MultiEngine runs FP32 problems on the batched path with boundary saving")
+        descs = (_lib.SwitDesc * len(views))(*[v._desc for v in views])
+        h = C.c_void_p()
+        _lib.check(lib.swit_multi_create(descs, len(views), C.byref(h)))
+        self._h, self._lib = h, lib
+        self.engines = []
+        for i, (v, p) in enumerate(zip(views, problems)):
+            e = C.c_void_p()
+            _lib.check(lib.swit_multi_engine(h, i, C.byref(e)))
+            v._h = e
+            self.engines.append(v)
+
+    def __len__(self):
+        return len(self.engines)
+
+    def _inputs(self, srcs, obss):
+        if len(srcs) != len(self) or len(obss) != len(self):
+            raise ValueError("one src and one obs per problem")
+        ps, po, keep, devs = [], [], [], set()
+        for e, s, o in zip(self.engines, srcs, obss):
+            s, o = e._f32(s), e._f32(o)
+            if tuple(s.shape) != (e.ns, e.nt) or tuple(o.shape) != (e.ns, e.ngmax, e.nt):
+                raise ValueError("src (ns, nt) and obs (ns, ng_max, nt) per problem")
+            a, d1 = e._ptr(s, np.float32)
+            b, d2 = e._ptr(o, np.float32)
+            ps.append(a)
+            po.append(b)
+            keep += [s, o]
+            devs |= {d1, d2}
+        if len(devs) != 1:
+            raise ValueError("all inputs must be host arrays or all device arrays")
+        dev = devs.pop()
+        return (C.c_void_p * len(self))(*ps), (C.c_void_p * len(self))(*po), dev, keep
+
+    def gradient_l2(self, srcs, obss):
+        """Waveform-misfit gradients of every problem: a list of dict(grad, illum_fw, illum_bk, misfit)."""
+        ps, po, dev, keep = self._inputs(srcs, obss)
+        outs = [[e._new((e.nx, e.nz), dev) for _ in range(3)] for e in self.engines]
+        arr = [(C.c_void_p * len(self))(*[e._ptr(o[j], e.out_dtype)[0] for e, o in zip(self.engines, outs)])
+               for j in range(3)]
+        m = (C.c_double * len(self))()
+        _lib.check(self._lib.swit_multi_gradient_l2(self._h, ps, po, arr[0], arr[1], arr[2], m, dev,
+                                                    Engine._stream(dev)))
+        return [dict(grad=o[0], illum_fw=o[1], illum_bk=o[2], misfit=m[i]) for i, o in enumerate(outs)]
+
+    def misfit_l2(self, srcs, obss):
+        """Waveform misfit of every problem (forward runs only)."""
+        ps, po, dev, keep = self._inputs(srcs, obss)
+        m = (C.c_double * len(self))()
+        _lib.check(self._lib.swit_multi_misfit_l2(self._h, ps, po, m, dev, Engine._stream(dev)))
+        return list(m)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            for e in self.engines:
+                e._h = None
+            self._lib.swit_multi_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
         self.close()
 
 
