@@ -46,8 +46,12 @@ def parse():
     ap.add_argument("--kernel", default="auto", choices=["auto", "fused", "split", "vec", "cluster", "hybrid", "band"])
     ap.add_argument("--no-tune", action="store_true", help="skip the launch-configuration autotuner")
     ap.add_argument("--no-extras", action="store_true", help="skip plain path, CPU baseline and kernel profile")
-    ap.add_argument("--workload", default="marmousi", choices=["marmousi", "large"],
-                    help="marmousi: 481x141 nt 4000 49 shots (the headline); large: 2001x601 nt 6000 200 shots")
+    ap.add_argument("--workload", default="marmousi", choices=["marmousi", "large", "multi"],
+                    help="marmousi: 481x141 nt 4000 49 shots (the headline); large: 2001x601 nt 6000 200 shots; "
+                         "multi: uneven independent FWI problems, L-BFGS on all at once vs one after another")
+    ap.add_argument("--instances", type=int, default=64, help="multi: problems")
+    ap.add_argument("--iters", type=int, default=5, help="multi: L-BFGS iterations")
+    ap.add_argument("--scale", type=float, default=1.0, help="multi: factor on shot counts and record lengths")
     ap.add_argument("--checkpoint", default="0",
                     help="memory strategy: 0 = boundary saving, k = checkpoints every k steps, auto = the interval "
                          "that minimises memory")
@@ -393,10 +397,118 @@ def run_mine(args):
         dist.destroy_process_group()
 
 
+def run_multi(args):
+    """Uneven multi-instance batch: L-BFGS (swit_gb300.optim) on every problem,
+    (a) all problems stepped together by one MultiEngine (fwi_lockstep), (b) one
+    problem after another on its own batched engine, (c) one after another on the
+    plain path (one shot per launch, no graph).  Reports L-BFGS iterations per
+    second of each and the largest difference between their final models."""
+    import torch
+
+    from swit_gb300 import Engine, MultiEngine, optim, precond, survey
+    probs = survey.config4_instances(args.instances, args.scale, args.scale)
+    srcs = [torch.from_numpy(p.source()).cuda() for p in probs]
+    vpmax = 5000.0
+
+    def prec(p, o):
+        return precond.grad_precond(o["grad"], o["illum_fw"], o["illum_bk"], p.nx, p.nz, vpmax, "Land", 0, 0.0, 0)
+
+    def model(p, v):
+        return v.reshape(p.nx, p.nz).float().contiguous()
+
+    me = MultiEngine([p.engine_args() for p in probs])
+    obss = []
+    for e, p, s in zip(me.engines, probs, srcs):
+        e.set_model(torch.from_numpy(p.vp_true).cuda(), torch.from_numpy(p.rho(p.vp_true)).cuda())
+        obss.append(e.forward(s, save_boundary=False))
+    rhos = [torch.from_numpy(p.rho(p.vp_true)).cuda() for p in probs]
+    v0s = [torch.from_numpy(p.vp_init).cuda().double().reshape(-1) for p in probs]
+
+    def set_all(vs):
+        for e, p, v, r in zip(me.engines, probs, vs, rhos):
+            e.set_model(model(p, v), r)
+
+    def objective_all(vs):
+        set_all(vs)
+        return [(o["misfit"], prec(p, o)) for p, o in zip(probs, me.gradient_l2(srcs, obss))]
+
+    def misfit_all(vs, active):
+        for e, p, v, r, a in zip(me.engines, probs, vs, rhos, active):
+            if a:
+                e.set_model(model(p, v), r)
+        return me.misfit_l2(srcs, obss, active)
+
+    # one gradient of every problem: together vs one engine after another (kernel efficiency alone)
+    set_all(v0s)
+    me.gradient_l2(srcs, obss)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    me.gradient_l2(srcs, obss)
+    torch.cuda.synchronize()
+    t_grad_multi = time.perf_counter() - t0
+    t_grad_seq = 0.0
+    for p, s, o, r, v0 in zip(probs, srcs, obss, rhos, v0s):
+        with Engine(**p.engine_args()) as e:
+            e.set_model(model(p, v0), r)
+            e.gradient_l2(s, o)
+            torch.cuda.synchronize()
+            t1 = time.perf_counter()
+            e.gradient_l2(s, o)
+            torch.cuda.synchronize()
+            t_grad_seq += time.perf_counter() - t1
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    sts, hists = optim.fwi_lockstep(v0s, objective_all, misfit_all, maxiter=args.iters, vpmax=vpmax, vpmin=1000.0)
+    torch.cuda.synchronize()
+    t_multi = time.perf_counter() - t0
+    me.close()
+
+    def one_by_one(path):
+        finals, t = [], 0.0
+        for p, s, o, r, v0 in zip(probs, srcs, obss, rhos, v0s):
+            with Engine(**p.engine_args(), path=path) as e:
+                def obj(v, e=e, p=p, s=s, o=o, r=r):
+                    e.set_model(model(p, v), r)
+                    out = e.gradient_l2(s, o)
+                    return out["misfit"], prec(p, out)
+
+                def mis(v, e=e, p=p, s=s, o=o, r=r):
+                    e.set_model(model(p, v), r)
+                    return e.misfit_l2(s, o)
+
+                torch.cuda.synchronize()
+                t1 = time.perf_counter()
+                st, _ = optim.fwi(v0, obj, mis, maxiter=args.iters, vpmax=vpmax, vpmin=1000.0)
+                torch.cuda.synchronize()
+                t += time.perf_counter() - t1
+                finals.append(st["v_now"])
+        return finals, t
+
+    fin_b, t_batched = one_by_one("batched")
+    fin_p, t_plain = one_by_one("plain")
+    diff = max(float((a["v_now"] - b).abs().max()) for a, b in zip(sts, fin_b))
+    diff_p = max(float((a["v_now"] - b).abs().max()) for a, b in zip(sts, fin_p))
+    n_it = args.instances * args.iters
+    line = {"metric": "multi-instance FWI: L-BFGS iterations/s over all problems", "value": n_it / t_multi,
+            "unit": "iterations/s", "n_gpus": 1, "higher_is_better": True, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": "uneven multi-instance batch", "instances": args.instances, "iters": args.iters,
+                       "shot_and_nt_scale": args.scale,
+                       "grids": [[p.nx, p.nz] for p in probs], "shots": [p.ns for p in probs],
+                       "nt": [p.nt for p in probs]},
+            "seconds": {"multi": t_multi, "sequential_batched": t_batched, "sequential_plain": t_plain,
+                        "one_gradient_each_multi": t_grad_multi, "one_gradient_each_sequential": t_grad_seq},
+            "speedup": {"vs_sequential_batched": t_batched / t_multi, "vs_sequential_plain": t_plain / t_multi},
+            "max_model_difference_m_s": {"vs_sequential_batched": diff, "vs_sequential_plain": diff_p},
+            "final_misfit_ratio": [h[-1]["f"] / h[0]["f"] if h[0]["f"] else None for h in hists]}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload == "multi":
+        run_multi(args)
     else:
         run_mine(args)
 

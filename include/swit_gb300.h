@@ -211,6 +211,12 @@ int swit_query(const swit_engine* e, int64_t* device_bytes, int32_t* shots_per_b
  * reference, whose CPU loops have no asynchronous copies. */
 int swit_check(swit_engine* e, void* stream);
 
+/* The Waveform misfit of swit_gradient_l2 alone: a forward run without strips,
+ * then the same per-trace sums (misfit.py:128-148), for line-search trials
+ * (inversion.py:274-350 evaluates misfits only).  Waits for the stream. */
+int swit_misfit_l2(swit_engine* e, const float* src, const float* obs, double* misfit, int32_t on_device,
+                   void* stream);
+
 /* ---- Many independent problems in one set of launches --------------------
  * A multi-instance engine holds n regular engines (one swit_desc each: FP32,
  * batched path, vec kernels, boundary saving; grids, shot counts and nt may all
@@ -235,10 +241,11 @@ int swit_multi_gradient_l2(swit_multi* m, const float* const* src, const float* 
                            void* const* illum_fw, void* const* illum_bk, double* misfit, int32_t on_device,
                            void* stream);
 
-/* Waveform misfit of every instance (forward runs only, no strips); misfit[n]
- * on the host (waits). */
-int swit_multi_misfit_l2(swit_multi* m, const float* const* src, const float* const* obs, double* misfit,
-                         int32_t on_device, void* stream);
+/* Waveform misfit of the instances with active[i] != 0 (all if active is NULL;
+ * the others do no work and get 0): forward runs only, no strips; misfit[n] on
+ * the host (waits).  src[i], obs[i] of inactive instances are not read. */
+int swit_multi_misfit_l2(swit_multi* m, const float* const* src, const float* const* obs, const int32_t* active,
+                         double* misfit, int32_t on_device, void* stream);
 
 int swit_multi_destroy(swit_multi* m);
 

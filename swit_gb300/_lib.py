@@ -16,7 +16,7 @@ ERRORS = {-1: "SWIT_E_ARG", -2: "SWIT_E_GEOM", -3: "SWIT_E_CFL", -4: "SWIT_E_MOD
 # every symbol include/swit_gb300.h declares
 EXPORTS = ("swit_create", "swit_set_model", "swit_forward", "swit_backward", "swit_gradient_l2",
            "swit_export_snapshot", "swit_import_snapshot", "swit_profile_kernels", "swit_query", "swit_destroy", "swit_last_error", "swit_damp_profile",
-           "swit_forward_shot_static", "swit_check", "swit_multi_create", "swit_multi_engine",
+           "swit_forward_shot_static", "swit_check", "swit_misfit_l2", "swit_multi_create", "swit_multi_engine",
            "swit_multi_gradient_l2", "swit_multi_misfit_l2", "swit_multi_destroy")
 
 
@@ -64,10 +64,11 @@ def load(build_if_missing: bool = True):
                         C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.POINTER(C.c_int32)], i),
         "swit_destroy": ([vp], i),
         "swit_check": ([vp, vp], i),
+        "swit_misfit_l2": ([vp, vp, vp, C.POINTER(C.c_double), C.c_int32, vp], i),
         "swit_multi_create": ([C.POINTER(SwitDesc), C.c_int32, C.POINTER(vp)], i),
         "swit_multi_engine": ([vp, C.c_int32, C.POINTER(vp)], i),
         "swit_multi_gradient_l2": ([vp, vp, vp, vp, vp, vp, C.POINTER(C.c_double), C.c_int32, vp], i),
-        "swit_multi_misfit_l2": ([vp, vp, vp, C.POINTER(C.c_double), C.c_int32, vp], i),
+        "swit_multi_misfit_l2": ([vp, vp, vp, vp, C.POINTER(C.c_double), C.c_int32, vp], i),
         "swit_multi_destroy": ([vp], i),
         "swit_last_error": ([], C.c_char_p),
         "swit_damp_profile": ([C.c_int32, C.c_int32, C.c_int32, C.c_float, C.c_float, vp], i),

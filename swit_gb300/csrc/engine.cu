@@ -1267,11 +1267,13 @@ int setup_cluster(swit_engine* e, int want) {
 // Many independent problems stepped together (kernels_multi.cuh).
 struct swit_multi {
   std::vector<swit_engine*> eng;  // owned, caller order
-  std::vector<int> order;         // caller indices by record length, longest first (table and list order)
-  int max_nt = 0, max_ns = 0;
+  std::vector<int> order;         // caller indices by record length, longest first (table order)
+  int max_nt = 0;
   Inst<float>* d_tab = nullptr;
-  uint64_t* d_list[4] = {nullptr, nullptr, nullptr, nullptr};
-  std::vector<int> act[4];  // active prefix: [k][s] at forward step s (k = 0, 1) or reverse index s (k = 2, 3)
+  uint32_t* d_list[4] = {nullptr, nullptr, nullptr, nullptr};
+  uint2* d_blocks[4] = {nullptr, nullptr, nullptr, nullptr};
+  int* d_on = nullptr;      // per table row: instance switched on for this call
+  std::vector<int> act[4];  // active blocks: [k][s] at forward step s (k = 0, 1) or reverse index s (k = 2, 3)
   cudaStream_t cap = nullptr;
   cudaGraphExec_t gf[2] = {nullptr, nullptr};
   cudaGraphExec_t gb = nullptr;
@@ -1285,15 +1287,18 @@ void multi_release(swit_multi* m) {
   if (m->gb) cudaGraphExecDestroy(m->gb);
   if (m->cap) cudaStreamDestroy(m->cap);
   if (m->d_tab) cudaFree(m->d_tab);
-  for (uint64_t* l : m->d_list)
-    if (l) cudaFree(l);
+  if (m->d_on) cudaFree(m->d_on);
+  for (int k = 0; k < 4; ++k) {
+    if (m->d_list[k]) cudaFree(m->d_list[k]);
+    if (m->d_blocks[k]) cudaFree(m->d_blocks[k]);
+  }
   for (swit_engine* e : m->eng) {
     release(e);
     delete e;
   }
 }
 
-// Combined task lists, active prefixes and the instance table.
+// Instance table, padded task lists, block tables and active prefixes.
 int multi_build(swit_multi* m) {
   const int n = (int)m->eng.size();
   m->order.resize(n);
@@ -1303,7 +1308,6 @@ int multi_build(swit_multi* m) {
   std::vector<Inst<float>> tab(n);
   for (int r = 0; r < n; ++r) {
     swit_engine* e = m->eng[m->order[r]];
-    m->max_ns = std::max(m->max_ns, e->ns);
     Inst<float>& I = tab[r];
     I.g = make_grid<float>(e);
     I.rec = make_rec(e);
@@ -1328,20 +1332,29 @@ int multi_build(swit_multi* m) {
   }
   CK(cudaMalloc(&m->d_tab, n * sizeof(Inst<float>)));
   CK(cudaMemcpy(m->d_tab, tab.data(), n * sizeof(Inst<float>), cudaMemcpyHostToDevice));
+  CK(cudaMalloc(&m->d_on, n * sizeof(int)));
   for (int k = 0; k < 4; ++k) {
-    std::vector<uint64_t> L;
+    std::vector<uint32_t> L;
+    std::vector<uint2> B;
     std::vector<int> cum(n);
     for (int r = 0; r < n; ++r) {
       const swit_engine* e = m->eng[m->order[r]];
       const uint32_t* src = &e->h_list[(size_t)k * e->list_stride];
+      const uint32_t base = (uint32_t)L.size();
       for (int i = 0; i < e->list_len[k]; ++i) {
-        const uint64_t t = i < e->list_n0[k] ? 0 : (i < e->list_n1[k] ? 1 : 2);
-        L.push_back(((uint64_t)r << 40) | (t << 32) | src[i]);
+        const uint32_t t = i < e->list_n0[k] ? 0u : (i < e->list_n1[k] ? 1u : 2u);
+        L.push_back((t << 30) | src[i]);
       }
-      cum[r] = (int)L.size();
+      while (L.size() % 256) L.push_back(kMultiPad);
+      const int chunks = (int)((L.size() - base) / 256);
+      for (int s = 0; s < e->ns; ++s)
+        for (int c = 0; c < chunks; ++c) B.push_back(make_uint2(((uint32_t)r << 16) | (uint32_t)s, base + 256u * c));
+      cum[r] = (int)B.size();
     }
-    CK(cudaMalloc(&m->d_list[k], std::max<size_t>(L.size(), 1) * sizeof(uint64_t)));
-    CK(cudaMemcpy(m->d_list[k], L.data(), L.size() * sizeof(uint64_t), cudaMemcpyHostToDevice));
+    CK(cudaMalloc(&m->d_list[k], std::max<size_t>(L.size(), 1) * sizeof(uint32_t)));
+    CK(cudaMemcpy(m->d_list[k], L.data(), L.size() * sizeof(uint32_t), cudaMemcpyHostToDevice));
+    CK(cudaMalloc(&m->d_blocks[k], std::max<size_t>(B.size(), 1) * sizeof(uint2)));
+    CK(cudaMemcpy(m->d_blocks[k], B.data(), B.size() * sizeof(uint2), cudaMemcpyHostToDevice));
     // instances with nt >= s run forward step s and reverse index s - 2: a prefix of the order
     m->act[k].assign(m->max_nt + 1, 0);
     for (int s = 2; s <= m->max_nt; ++s) {
@@ -1359,28 +1372,30 @@ int multi_build(swit_multi* m) {
 }
 
 // The forward (which = 0: no strips, 1: with strips) or reverse (which = 2)
-// loop of every instance, one launch per phase and step, captured once.
-int multi_loop(swit_multi* m, int which, cudaStream_t st) {
+// loop of every switched-on instance, one launch per phase and step, captured
+// once.  on[i] (caller order) switches instance i on for this call.
+int multi_loop(swit_multi* m, int which, const std::vector<int>& on, cudaStream_t st) {
+  std::vector<int> rows(m->eng.size());
+  for (size_t r = 0; r < rows.size(); ++r) rows[r] = on[m->order[r]];
+  CK(cudaMemcpyAsync(m->d_on, rows.data(), rows.size() * sizeof(int), cudaMemcpyHostToDevice, st));
   cudaGraphExec_t& ex = which == 2 ? m->gb : m->gf[which];
   if (!ex) {
     cudaGraph_t graph;
     CK(cudaStreamBeginCapture(m->cap, cudaStreamCaptureModeThreadLocal));
     const dim3 block(256);
-    auto grid = [&](int len) { return dim3((unsigned)std::max(1, (len + 255) / 256), (unsigned)m->max_ns); };
     const Inst<float>* tab = m->d_tab;
+    auto ml = [&](int k, int nb) { return MultiLaunch{m->d_blocks[k], m->d_list[k], m->d_on, nb}; };
+    auto grid = [](int nb) { return dim3((unsigned)std::max(1, nb)); };
     if (which < 2) {
       for (int it = 2; it <= m->max_nt; ++it) {
-        launch_pdl(true, k_fwd_p_m<float>, grid(m->act[0][it]), block, m->cap, tab, (const uint64_t*)m->d_list[0],
-                   m->act[0][it], it);
-        launch_pdl(true, k_fwd_uw_m<float>, grid(m->act[1][it]), block, m->cap, tab, (const uint64_t*)m->d_list[1],
-                   m->act[1][it], it, which);
+        launch_pdl(true, k_fwd_p_m<float>, grid(m->act[0][it]), block, m->cap, tab, ml(0, m->act[0][it]), it);
+        launch_pdl(true, k_fwd_uw_m<float>, grid(m->act[1][it]), block, m->cap, tab, ml(1, m->act[1][it]), it,
+                   which);
       }
     } else {
       for (int jr = 0; jr <= m->max_nt - 2; ++jr) {
-        launch_pdl(true, k_bwd_uw_m<float>, grid(m->act[2][jr]), block, m->cap, tab, (const uint64_t*)m->d_list[2],
-                   m->act[2][jr], jr);
-        launch_pdl(true, k_bwd_p_m<float>, grid(m->act[3][jr]), block, m->cap, tab, (const uint64_t*)m->d_list[3],
-                   m->act[3][jr], jr);
+        launch_pdl(true, k_bwd_uw_m<float>, grid(m->act[2][jr]), block, m->cap, tab, ml(2, m->act[2][jr]), jr);
+        launch_pdl(true, k_bwd_p_m<float>, grid(m->act[3][jr]), block, m->cap, tab, ml(3, m->act[3][jr]), jr);
       }
     }
     cudaError_t rc = cudaStreamEndCapture(m->cap, &graph);
@@ -1770,12 +1785,26 @@ int swit_check(swit_engine* e, void* stream) {
   return 0;
 }
 
+int swit_misfit_l2(swit_engine* e, const float* src, const float* obs, double* misfit, int32_t on_device,
+                   void* stream) {
+  if (!e || !src || !obs || !misfit) return fail(SWIT_E_ARG, "null argument");
+  if (!e->model_set) return fail(SWIT_E_STATE, "swit_set_model has not been called");
+  cudaStream_t st = (cudaStream_t)stream;
+  int rc = e->prec ? forward_impl<double>(e, src, nullptr, false, on_device, st)
+                   : forward_impl<float>(e, src, nullptr, false, on_device, st);
+  if (rc) return rc;
+  rc = e->prec ? residual_l2<double>(e, obs, on_device, st) : residual_l2<float>(e, obs, on_device, st);
+  if (rc) return rc;
+  return misfit_sum(e, st, misfit);
+}
+
 int swit_multi_create(const swit_desc* descs, int32_t n, swit_multi** out) {
   if (!descs || !out || n < 1) return fail(SWIT_E_ARG, "null argument or no instance");
   if (n > 65535) return fail(SWIT_E_LIMIT, "at most 65535 instances");
   *out = nullptr;
   for (int i = 0; i < n; ++i) {
     const swit_desc& d = descs[i];
+    if (d.nx + 2 * d.npml > 16384 || d.ns > 65535) return fail(SWIT_E_LIMIT, "instance %d: more than 16384 PML-grid columns", i);
     if (d.precision != 0 || d.path != 0 || (d.kernel_variant != 0 && d.kernel_variant != 3) || d.checkpoint_every)
       return fail(SWIT_E_ARG,
                   "instance %d: a multi-instance engine runs FP32 vec kernels on the batched path with boundary saving",
@@ -1821,13 +1850,14 @@ int swit_multi_gradient_l2(swit_multi* m, const float* const* src, const float* 
     int rc = forward_impl<float>(m->eng[i], src[i], nullptr, true, on_device, st, false);
     if (rc) return rc;
   }
-  int rc = multi_loop(m, 1, st);
+  const std::vector<int> all(n, 1);
+  int rc = multi_loop(m, 1, all, st);
   if (rc) return rc;
   for (int i = 0; i < n; ++i) {
     if ((rc = residual_l2<float>(m->eng[i], obs[i], on_device, st))) return rc;
     if ((rc = backward_begin<float>(m->eng[i], st))) return rc;
   }
-  if ((rc = multi_loop(m, 2, st))) return rc;
+  if ((rc = multi_loop(m, 2, all, st))) return rc;
   for (int i = 0; i < n; ++i) {
     rc = backward_end<float>(m->eng[i], grad ? grad[i] : nullptr, illum_fw ? illum_fw[i] : nullptr,
                              illum_bk ? illum_bk[i] : nullptr, on_device, st);
@@ -1839,23 +1869,30 @@ int swit_multi_gradient_l2(swit_multi* m, const float* const* src, const float* 
   return 0;
 }
 
-int swit_multi_misfit_l2(swit_multi* m, const float* const* src, const float* const* obs, double* misfit,
-                         int32_t on_device, void* stream) {
+int swit_multi_misfit_l2(swit_multi* m, const float* const* src, const float* const* obs, const int32_t* active,
+                         double* misfit, int32_t on_device, void* stream) {
   if (!m || !src || !obs || !misfit) return fail(SWIT_E_ARG, "null argument");
   cudaStream_t st = (cudaStream_t)stream;
   const int n = (int)m->eng.size();
+  std::vector<int> on(n, 1);
+  if (active)
+    for (int i = 0; i < n; ++i) on[i] = active[i] ? 1 : 0;
   for (int i = 0; i < n; ++i)
-    if (!m->eng[i]->model_set) return fail(SWIT_E_STATE, "instance %d: swit_set_model has not been called", i);
+    if (on[i] && !m->eng[i]->model_set)
+      return fail(SWIT_E_STATE, "instance %d: swit_set_model has not been called", i);
   for (int i = 0; i < n; ++i) {
+    if (!on[i]) continue;
     int rc = forward_impl<float>(m->eng[i], src[i], nullptr, false, on_device, st, false);
     if (rc) return rc;
   }
-  int rc = multi_loop(m, 0, st);
+  int rc = multi_loop(m, 0, on, st);
   if (rc) return rc;
   for (int i = 0; i < n; ++i)
-    if ((rc = residual_l2<float>(m->eng[i], obs[i], on_device, st))) return rc;
-  for (int i = 0; i < n; ++i)
-    if ((rc = misfit_sum(m->eng[i], st, &misfit[i]))) return rc;
+    if (on[i] && (rc = residual_l2<float>(m->eng[i], obs[i], on_device, st))) return rc;
+  for (int i = 0; i < n; ++i) {
+    misfit[i] = 0.0;
+    if (on[i] && (rc = misfit_sum(m->eng[i], st, &misfit[i]))) return rc;
+  }
   return 0;
 }
 

@@ -3,15 +3,16 @@
 //
 // Each instance is a regular engine (its own arrays); a device table holds per
 // instance the grid description, receiver and source tables and array
-// pointers.  One combined task list per phase kernel concatenates the
-// instances' own task lists (kernels_vec.cuh), instances ordered by record
-// length nt, longest first, each entry (instance << 40 | tier << 32 |
-// (ix - 1) << 16 | q).  All forward loops start together and all reverse loops
-// start together, so at a given step the instances still running are a prefix
-// of the list and a launch covers exactly that prefix.  blockIdx.y is the
-// shot; threads past an instance's shot count return at once.  The vector
-// bodies are those of the single-instance kernels, so every instance computes
-// the bits its own engine would.
+// pointers.  Per phase kernel, every instance's own task list (kernels_vec.cuh)
+// is padded to whole blocks of 256 entries and the blocks of all instances and
+// shots are listed in a block table, instances ordered by record length nt,
+// longest first.  All forward loops start together and all reverse loops start
+// together, so at a given step the blocks of the instances still running are a
+// prefix of the block table and a launch covers exactly that prefix.  A block
+// belongs to one instance and one shot: it stages the instance's description in
+// shared memory once, and skips its work when the instance is switched off for
+// this call.  The vector bodies are those of the single-instance kernels, so
+// every instance computes the bits its own engine would.
 #pragma once
 #include "kernels_vec.cuh"
 
@@ -29,78 +30,87 @@ struct Inst {
   const R* adj_t;
 };
 
-// List entry i -> instance, vector index set and tier; null past the active
-// prefix or past the instance's shots.
+constexpr uint32_t kMultiPad = 0xffffffffu;  // padding entry of a block
+
+// Block table entry: x = instance << 16 | shot, y = first list entry of the block.
+// List entries: tier << 30 | (ix - 1) << 16 | q, or kMultiPad.
+struct MultiLaunch {
+  const uint2* __restrict__ blocks;
+  const uint32_t* __restrict__ list;
+  const int* __restrict__ on;  // per instance: 0 = skip in this call
+  int nblocks;                 // active prefix
+};
+
+// Stages this block's instance description in shared memory; returns it, or
+// null when the block is past the active prefix or its instance is off (uniform
+// over the block).  *e = this thread's list entry.
 template <class R>
-__device__ __forceinline__ const Inst<R>* multi_index(const Inst<R>* __restrict__ tab,
-                                                       const uint64_t* __restrict__ list, int len, VecIdx& v, int& t) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= len) return nullptr;
-  const uint64_t e = list[i];
-  const Inst<R>* I = tab + (e >> 40);
-  const int s = blockIdx.y;
-  if (s >= I->ns) return nullptr;
-  t = (int)((e >> 32) & 3u);
+__device__ __forceinline__ const Inst<R>* multi_block(const Inst<R>* __restrict__ tab, const MultiLaunch& L,
+                                                      Inst<R>* sI, uint32_t* e, int* s) {
+  if ((int)blockIdx.x >= L.nblocks) return nullptr;
+  const uint2 b = L.blocks[blockIdx.x];
+  const int r = (int)(b.x >> 16);
+  if (!L.on[r]) return nullptr;
+  *s = (int)(b.x & 0xffffu);
+  *e = L.list[b.y + threadIdx.x];
+  const int* src = reinterpret_cast<const int*>(tab + r);
+  int* dst = reinterpret_cast<int*>(sI);
+  for (int k = threadIdx.x; k < (int)(sizeof(Inst<R>) / sizeof(int)); k += blockDim.x) dst[k] = src[k];
+  __syncthreads();
+  return sI;
+}
+
+__device__ __forceinline__ void multi_vec(const int LD, uint32_t e, int s, VecIdx& v, int& t) {
+  t = (int)(e >> 30);
   v.s = s;
-  v.ix = (int)((e >> 16) & 0xffffu) + 1;
+  v.ix = (int)((e >> 16) & 0x3fffu) + 1;
   v.q = (int)(e & 0xffffu);
   v.iz0 = 4 * v.q + 1;
   v.ok = true;
-  v.k4 = (size_t)(v.ix - 1) * (I->g.LD >> 2) + v.q;
+  v.k4 = (size_t)(v.ix - 1) * (LD >> 2) + v.q;
   v.kc = v.k4;
   v.kg = v.k4;
-  return I;
 }
+
+// The instance description is a block-uniform early exit, so __syncthreads in
+// multi_block is reached by all threads or none.
+#define SWIT_MULTI_PROLOGUE                                          \
+  __shared__ __align__(16) unsigned char inst_sm[sizeof(Inst<R>)];   \
+  uint32_t e = kMultiPad;                                            \
+  int s = 0;                                                         \
+  const Inst<R>* I = multi_block(tab, L, reinterpret_cast<Inst<R>*>(inst_sm), &e, &s); \
+  pdl_enter();                                                       \
+  if (!I || e == kMultiPad) return;                                  \
+  VecIdx v;                                                          \
+  int t;                                                             \
+  multi_vec(I->g.LD, e, s, v, t);                                    \
+  const size_t off = (size_t)s * I->g.FSZ;
 
 // Forward phases at step it (the same step for every running instance).
 template <class R>
-__global__ void __launch_bounds__(256) k_fwd_p_m(const Inst<R>* __restrict__ tab, const uint64_t* __restrict__ list,
-                                                 int len, int it) {
-  VecIdx v;
-  int t;
-  const Inst<R>* I = multi_index(tab, list, len, v, t);
-  pdl_enter();
-  if (!I) return;
-  const size_t off = (size_t)v.s * I->g.FSZ;
+__global__ void __launch_bounds__(256) k_fwd_p_m(const Inst<R>* __restrict__ tab, MultiLaunch L, int it) {
+  SWIT_MULTI_PROLOGUE
   SWIT_TIER_CALL(fwd_p_body, I->g, I->src, I->s_fwd, I->p + off, I->u + off, I->w + off, it, v);
 }
 
 template <class R>
-__global__ void __launch_bounds__(256) k_fwd_uw_m(const Inst<R>* __restrict__ tab, const uint64_t* __restrict__ list,
-                                                  int len, int it, int store) {
-  VecIdx v;
-  int t;
-  const Inst<R>* I = multi_index(tab, list, len, v, t);
-  pdl_enter();
-  if (!I) return;
-  const size_t off = (size_t)v.s * I->g.FSZ;
+__global__ void __launch_bounds__(256) k_fwd_uw_m(const Inst<R>* __restrict__ tab, MultiLaunch L, int it, int store) {
+  SWIT_MULTI_PROLOGUE
   SWIT_TIER_CALL(fwd_uw_body, I->g, I->rec, I->p + off, I->u + off, I->w + off, I->seis_t, store ? I->strips : nullptr,
                  it, v);
 }
 
 // Reverse phases at reverse index jr: instance step it = nt - jr.
 template <class R>
-__global__ void __launch_bounds__(256) k_bwd_uw_m(const Inst<R>* __restrict__ tab, const uint64_t* __restrict__ list,
-                                                  int len, int jr) {
-  VecIdx v;
-  int t;
-  const Inst<R>* I = multi_index(tab, list, len, v, t);
-  pdl_enter();
-  if (!I) return;
-  const size_t off = (size_t)v.s * I->g.FSZ;
+__global__ void __launch_bounds__(256) k_bwd_uw_m(const Inst<R>* __restrict__ tab, MultiLaunch L, int jr) {
+  SWIT_MULTI_PROLOGUE
   SWIT_TIER_CALL(bwd_uw_body, I->g, I->pb + off, I->ub + off, I->wb + off, I->pe + off, I->ue + off, I->we + off,
                  I->strips, I->g.nt - jr, v);
 }
 
 template <class R>
-__global__ void __launch_bounds__(256) k_bwd_p_m(const Inst<R>* __restrict__ tab, const uint64_t* __restrict__ list,
-                                                 int len, int jr) {
-  VecIdx v;
-  int t;
-  const Inst<R>* I = multi_index(tab, list, len, v, t);
-  pdl_enter();
-  if (!I) return;
-  const size_t off = (size_t)v.s * I->g.FSZ;
+__global__ void __launch_bounds__(256) k_bwd_p_m(const Inst<R>* __restrict__ tab, MultiLaunch L, int jr) {
+  SWIT_MULTI_PROLOGUE
   SWIT_TIER_CALL(bwd_p_body, I->g, I->rec, I->src, I->s_fwd, I->adj_t, I->pb + off, I->ub + off, I->wb + off,
                  I->pe + off, I->ue + off, I->we + off, I->dg + off, I->dfw + off, I->dbk + off, I->strips,
                  I->g.nt - jr, v);

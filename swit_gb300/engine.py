@@ -163,6 +163,17 @@ class Engine:
             out["seis"] = seis
         return out
 
+    def misfit_l2(self, src, obs):
+        """Waveform misfit only (a forward run without strips; swit_misfit_l2)."""
+        src, obs = self._f32(src), self._f32(obs)
+        ps, dev = self._ptr(src, np.float32)
+        po, dev2 = self._ptr(obs, np.float32)
+        if dev != dev2:
+            raise ValueError("src and obs must both be host or both be device arrays")
+        m = C.c_double(0.0)
+        _lib.check(self._lib.swit_misfit_l2(self._h, ps, po, C.byref(m), dev, self._stream(dev)))
+        return m.value
+
     def export_snapshot(self):
         """Boundary strips (ns, nt, 9nx+6nz) and p_end/u_end/w_end (ns, nx, nz) of the last saved forward."""
         b = np.zeros((self.ns, self.nt, 9 * self.nx + 6 * self.nz), self.out_dtype)
@@ -285,11 +296,13 @@ class MultiEngine:
                                                     Engine._stream(dev)))
         return [dict(grad=o[0], illum_fw=o[1], illum_bk=o[2], misfit=m[i]) for i, o in enumerate(outs)]
 
-    def misfit_l2(self, srcs, obss):
-        """Waveform misfit of every problem (forward runs only)."""
+    def misfit_l2(self, srcs, obss, active=None):
+        """Waveform misfit of every problem with active[i] true (all by default;
+        the others do no work and get 0): forward runs only."""
         ps, po, dev, keep = self._inputs(srcs, obss)
+        act = None if active is None else (C.c_int32 * len(self))(*[1 if a else 0 for a in active])
         m = (C.c_double * len(self))()
-        _lib.check(self._lib.swit_multi_misfit_l2(self._h, ps, po, m, dev, Engine._stream(dev)))
+        _lib.check(self._lib.swit_multi_misfit_l2(self._h, ps, po, act, m, dev, Engine._stream(dev)))
         return list(m)
 
     def close(self):

@@ -112,9 +112,9 @@ def lbfgs_direction(st):
     return st
 
 
-def backtrack(st, misfit_of, step_length, vpmax, vpmin, dec=0.5, search_max=6, vmax_thresh=300.0,
-              vmin_thresh=20.0):
-    """inversion.py:274-350; misfit_of(v) evaluates the misfit of a trial model vector."""
+def backtrack_steps(st, step_length, vpmax, vpmin, dec=0.5, search_max=6, vmax_thresh=300.0, vmin_thresh=20.0):
+    """inversion.py:274-350 as a generator: yields each trial model vector, is sent
+    its misfit, and returns the updated state (StopIteration.value)."""
     v_now, d_now, f_now = st["v_now"], st["d_now"], st["f_now"]
     if st["scheme"] == "LBFGS" and st["lbfgs_it"] != 1:
         dmax = float(d_now.abs().max())
@@ -125,7 +125,7 @@ def backtrack(st, misfit_of, step_length, vpmax, vpmin, dec=0.5, search_max=6, v
     while True:
         ls_iter += 1
         v_try = model_update(v_now, d_now * step, vpmax, vpmin)
-        f_try = float(misfit_of(v_try))
+        f_try = float((yield v_try))
         if f_try < f_now:
             st.update(ls_status=0, ls_iter=ls_iter, ls_step=step, f_try=f_try, v_try=v_try)
             st["log"].append("line search: step = %.4f, f_now = %.4e, f_try = %.4e. Succeed." % (step, f_now, f_try))
@@ -136,6 +136,18 @@ def backtrack(st, misfit_of, step_length, vpmax, vpmin, dec=0.5, search_max=6, v
             st["log"].append("line search fails: exceed the iteration of linesearch.")
             return st
         step = step * dec
+
+
+def backtrack(st, misfit_of, step_length, vpmax, vpmin, dec=0.5, search_max=6, vmax_thresh=300.0,
+              vmin_thresh=20.0):
+    """inversion.py:274-350; misfit_of(v) evaluates the misfit of a trial model vector."""
+    gen = backtrack_steps(st, step_length, vpmax, vpmin, dec, search_max, vmax_thresh, vmin_thresh)
+    v = next(gen)
+    while True:
+        try:
+            v = gen.send(misfit_of(v))
+        except StopIteration as done:
+            return done.value
 
 
 def decide(st):
@@ -180,3 +192,46 @@ def fwi(v0, objective, misfit_of, scheme="LBFGS", maxiter=5, step_length=0.02, v
         st = decide(st)
         hist.append(dict(iteration=it, f=st["f_now"], step=st["ls_step"], ls_status=st["ls_status"]))
     return st, hist
+
+
+def fwi_lockstep(v0s, objective_all, misfit_all, scheme="LBFGS", maxiter=5, step_length=0.02, vpmax=5000.0,
+                 vpmin=1000.0):
+    """fwi for many independent problems at once: each iteration evaluates every
+    problem's objective in one call, then runs the problems' line searches in
+    lockstep rounds, one misfit_all call per round.  objective_all(vs) ->
+    [(f, g)]; misfit_all(vs, active) -> [f], where only the problems with
+    active[i] true are still searching (the others' values are not used).  Every problem follows the same iterates as fwi()
+    would give it alone.  Returns (states, histories)."""
+    sts, hists = [], []
+    for v0 in v0s:
+        v0 = torch.as_tensor(v0, dtype=torch.float64)
+        st = init_state(scheme, v0.numel(), device=v0.device)
+        st["v_now"] = v0.clone()
+        st["v_old"] = v0.clone()
+        sts.append(st)
+        hists.append([])
+    for it in range(1, maxiter + 1):
+        fg = objective_all([st["v_now"] for st in sts])
+        gens, trials, active = [], [], []
+        for st, (f, g) in zip(sts, fg):
+            st["f_now"], st["g_now"] = float(f), torch.as_tensor(g, dtype=torch.float64, device=st["v_now"].device)
+            st = nlcg_direction(st) if scheme == "NLCG" else lbfgs_direction(st)
+            gen = backtrack_steps(st, step_length, vpmax, vpmin)
+            gens.append(gen)
+            trials.append(next(gen))
+            active.append(True)
+        while any(active):
+            fs = misfit_all(trials, list(active))
+            for i in range(len(sts)):
+                if not active[i]:
+                    continue
+                try:
+                    trials[i] = gens[i].send(fs[i])
+                except StopIteration as done:
+                    sts[i] = done.value
+                    active[i] = False
+        for i in range(len(sts)):
+            sts[i] = decide(sts[i])
+            hists[i].append(dict(iteration=it, f=sts[i]["f_now"], step=sts[i]["ls_step"],
+                                 ls_status=sts[i]["ls_status"]))
+    return sts, hists

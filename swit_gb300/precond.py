@@ -14,30 +14,31 @@ import torch
 import torch.nn.functional as F
 
 
-def _gauss_kernel(span, dtype, device):
-    """tools.py:255-269: exp(-x^2/(2 span^2) - y^2/(2 span^2)) / (2 pi span^2) on
-    x, y = linspace(-2 span, 2 span, 2 span + 1), normalised to sum 1."""
+def _gauss_1d(span, dtype, device):
+    """One factor of the kernel of tools.py:255-269: exp(-x^2 / (2 span^2)) on
+    x = linspace(-2 span, 2 span, 2 span + 1), normalised to sum 1.  The 2-D kernel
+    exp(-0.5 (X^2 + Y^2) / span^2) / (2 pi span^2), normalised to sum 1, is the outer
+    product of two of these (the constant cancels in the normalisation)."""
     x = torch.linspace(-2.0 * span, 2.0 * span, 2 * span + 1, dtype=torch.float64, device=device)
-    X, Y = torch.meshgrid(x, x, indexing="xy")
-    s2 = float(span) ** 2
-    Z = torch.exp(-0.5 * (X ** 2 / s2 + Y ** 2 / s2)) * (2.0 * math.pi * math.sqrt(s2 * s2)) ** -1.0
-    return (Z / Z.sum()).to(dtype)
+    a = torch.exp(-0.5 * x ** 2 / float(span) ** 2)
+    return (a / a.sum()).to(dtype)
 
 
-def _conv_same(Z, K):
-    """scipy.signal.convolve2d(Z, K, 'same') with zero fill (K has odd sides)."""
-    kh, kw = K.shape
-    out = F.conv2d(Z[None, None], torch.flip(K, (0, 1))[None, None], padding=(kh // 2, kw // 2))
+def _conv_same(Z, k):
+    """scipy.signal.convolve2d(Z, outer(k, k), 'same') with zero fill, as a 1-D
+    convolution along each axis (k symmetric, odd length)."""
+    n = k.numel()
+    out = F.conv2d(Z[None, None], k.view(1, 1, n, 1), padding=(n // 2, 0))
+    out = F.conv2d(out, k.view(1, 1, 1, n), padding=(0, n // 2))
     return out[0, 0]
 
 
 def smooth2d(Z, span=10):
     """tools.py:255-275: Gaussian smoothing, normalised by the smoothed ones array."""
     Z = torch.as_tensor(Z, dtype=torch.float64)
-    K = _gauss_kernel(int(span), Z.dtype, Z.device)
-    # meshgrid(x, y) in the reference puts x along columns: K[i, j] = f(y_i, x_j), symmetric anyway
-    num = _conv_same(Z, K)
-    den = _conv_same(torch.ones_like(Z), K)
+    k = _gauss_1d(int(span), Z.dtype, Z.device)
+    num = _conv_same(Z, k)
+    den = _conv_same(torch.ones_like(Z), k)
     return num / den
 
 

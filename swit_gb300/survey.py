@@ -182,6 +182,29 @@ def config(idx, ns=None, nt=None):
                   vp_true=vp, vp_init=init, src_xz=src, rec_xz=rec)
 
 
+def config4_instances(n=64, shot_scale=1.0, nt_scale=1.0, npml=40):
+    """The uneven multi-instance batch: instance i (seed 2000 + i) has nx, nz drawn
+    from [201, 801] x [101, 301], dx from {10, 20, 25} m, a Ricker of 3-12 Hz, nt
+    from [1500, 5000], 8-64 shots and one receiver per surface cell, vp from the
+    layered + anomaly generator, dt = 0.5 dx / vmax (CFL 0.5).  shot_scale and
+    nt_scale shrink the shot counts and record lengths of a bounded sample."""
+    out = []
+    for i in range(n):
+        rng = np.random.default_rng(2000 + i)
+        nx, nz = int(rng.integers(201, 802)), int(rng.integers(101, 302))
+        dx = float(rng.choice([10.0, 20.0, 25.0]))
+        f0 = float(rng.uniform(3.0, 12.0))
+        nt = max(50, int(round(int(rng.integers(1500, 5001)) * nt_scale)))
+        ns = max(1, int(round(int(rng.integers(8, 65)) * shot_scale)))
+        vp = layered_anomaly(nx, nz, dx, seed=2000 + i)
+        dt = float(np.float32(0.5 * dx / float(vp.max())))
+        src, rec = _line_geometry(nx, dx, ns, 2 * dx, 2 * dx, ng=nx)
+        out.append(Survey(name="instance %d %dx%d dx%g nt%d %d shots" % (i, nx, nz, dx, nt, ns), nx=nx, nz=nz,
+                          dx=dx, dt=dt, nt=nt, npml=npml, f0=f0, vp_true=vp, vp_init=smooth(vp, 250.0, dx),
+                          src_xz=src, rec_xz=rec))
+    return out
+
+
 def small(nx=48, nz=32, npml=10, nt=300, dx=10.0, dt=0.001, ns=3, ng=None, seed=7, zs=20.0, zr=10.0):
     """A small seeded problem for parity tests (layered + anomalies, a few shots)."""
     vp = layered_anomaly(nx, nz, dx, seed=seed, n_anom=3, vtop=1800.0, vbot=3200.0)

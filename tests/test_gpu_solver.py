@@ -191,8 +191,25 @@ def test_multi_engine_matches_each_engine_bit_for_bit():
                 assert o["misfit"] == r["misfit"]
         mis = me.misfit_l2(srcs, obss)
         assert mis == [r[1]["misfit"] for r in ref]
+        mis = me.misfit_l2(srcs, obss, active=[False, True, False])
+        assert mis == [0.0, ref[1][1]["misfit"], 0.0]
+        outs = me.gradient_l2(srcs, obss)  # every instance again after a partial call
+        for o, (_, r) in zip(outs, ref):
+            np.testing.assert_array_equal(o["grad"], r["grad"])
         # device inputs
         outs = me.gradient_l2([torch.from_numpy(x).cuda() for x in srcs], [torch.from_numpy(x).cuda() for x in obss])
         torch.cuda.synchronize()
         for o, (_, r) in zip(outs, ref):
             np.testing.assert_array_equal(o["grad"].cpu().numpy(), r["grad"])
+
+
+def test_misfit_only_call_matches_the_gradient_call():
+    s = survey.small()
+    rho = s.rho(s.vp_true)
+    with Engine(**s.engine_args()) as e:
+        e.set_model(s.vp_true, rho)
+        obs = e.forward(s.source(), save_boundary=False)
+        e.set_model(s.vp_init, rho)
+        m = e.misfit_l2(s.source(), obs)
+        r = e.gradient_l2(s.source(), obs)
+    assert m == r["misfit"] and m > 0

@@ -55,3 +55,37 @@ def test_model_update_clips_to_bounds():
     v = torch.tensor([1000.0, 2000.0, 4900.0])
     out = O.model_update(v, torch.tensor([-500.0, 10.0, 500.0]), 5000.0, 1000.0)
     assert out.tolist() == [1000.0, 2010.0, 5000.0]
+
+
+@pytest.mark.parametrize("scheme", ["LBFGS", "NLCG"])
+def test_lockstep_fwi_follows_each_problem_alone(scheme):
+    """Three independent quadratic problems run through fwi_lockstep take the same
+    iterates, line-search steps and misfits as fwi runs each alone."""
+    rng = np.random.default_rng(5)
+    probs = []
+    for n in (30, 45, 20):
+        Q = rng.standard_normal((n, n))
+        A = torch.tensor(Q @ Q.T / n + np.eye(n))
+        b = torch.tensor(rng.standard_normal(n))
+        v0 = torch.tensor(2000.0 + 100.0 * rng.standard_normal(n))
+        probs.append((A, b, v0))
+
+    def f_of(A, b, v):
+        return float(0.5 * v @ (A @ v) - b @ v)
+
+    def g_of(A, b, v):
+        return A @ v - b
+
+    alone = []
+    for A, b, v0 in probs:
+        st, h = O.fwi(v0, lambda v, A=A, b=b: (f_of(A, b, v), g_of(A, b, v)), lambda v, A=A, b=b: f_of(A, b, v),
+                          scheme=scheme, maxiter=4, vpmax=5000.0, vpmin=1000.0)
+        alone.append((st, h))
+    sts, hists = O.fwi_lockstep(
+        [p[2] for p in probs],
+        lambda vs: [(f_of(A, b, v), g_of(A, b, v)) for (A, b, _), v in zip(probs, vs)],
+        lambda vs, act: [f_of(A, b, v) if a else None for (A, b, _), v, a in zip(probs, vs, act)],
+        scheme=scheme, maxiter=4, vpmax=5000.0, vpmin=1000.0)
+    for (st, h), st2, h2 in zip(alone, sts, hists):
+        assert h == h2
+        assert torch.equal(st["v_now"], st2["v_now"])
