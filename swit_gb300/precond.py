@@ -11,7 +11,6 @@ The figure the reference draws of the illuminations is not reproduced.
 import math
 
 import torch
-import torch.nn.functional as F
 
 
 def _gauss_1d(span, dtype, device):
@@ -24,13 +23,29 @@ def _gauss_1d(span, dtype, device):
     return (a / a.sum()).to(dtype)
 
 
+_toeplitz = {}
+
+
+def _band(n, k):
+    """(n, n) matrix T with T[i, j] = k[j - i + r] for |j - i| <= r (r = len(k) // 2),
+    so T @ x is the zero-filled 'same' convolution of x with the symmetric k."""
+    key = (n, k.numel(), k.dtype, str(k.device), float(k[0]))
+    T = _toeplitz.get(key)
+    if T is None:
+        r = k.numel() // 2
+        i = torch.arange(n, device=k.device)
+        d = i[None, :] - i[:, None] + r
+        T = torch.where((d >= 0) & (d <= 2 * r), k[d.clamp(0, 2 * r)], torch.zeros((), dtype=k.dtype, device=k.device))
+        if len(_toeplitz) > 64:
+            _toeplitz.clear()
+        _toeplitz[key] = T
+    return T
+
+
 def _conv_same(Z, k):
-    """scipy.signal.convolve2d(Z, outer(k, k), 'same') with zero fill, as a 1-D
-    convolution along each axis (k symmetric, odd length)."""
-    n = k.numel()
-    out = F.conv2d(Z[None, None], k.view(1, 1, n, 1), padding=(n // 2, 0))
-    out = F.conv2d(out, k.view(1, 1, 1, n), padding=(0, n // 2))
-    return out[0, 0]
+    """scipy.signal.convolve2d(Z, outer(k, k), 'same') with zero fill: one banded
+    matrix product per axis (k symmetric, odd length)."""
+    return _band(Z.shape[0], k) @ Z @ _band(Z.shape[1], k).T
 
 
 def smooth2d(Z, span=10):
