@@ -26,8 +26,9 @@ def candidates(ns, nz_pml):
         for tx in (8, 16, 32):
             for b in batches:
                 out.append(dict(kernel="fused", block_x=tx, shots_per_batch=b))
-    for bx in (1, 2, 4, 8):
-        for b in batches[:2]:
+    vb = sorted({ns, max(1, -(-ns // 2)), max(1, -(-ns // 4)), max(1, -(-ns // 8))}, reverse=True)
+    for bx in (2, 4):
+        for b in vb:
             out.append(dict(kernel="vec", block_x=bx, shots_per_batch=b))
     out.append(dict(kernel="split", block_x=4, shots_per_batch=ns))
     out.append(dict(kernel="cluster", block_x=8, shots_per_batch=ns))
