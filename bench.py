@@ -43,6 +43,7 @@ def parse():
     ap.add_argument("--nt", type=int, default=None, help="time steps (default 4000)")
     ap.add_argument("--batch", type=int, default=0, help="shots per launch (0 = engine default)")
     ap.add_argument("--block-x", type=int, default=0)
+    ap.add_argument("--branches", type=int, default=0, help="concurrent graph branches (0 = engine default)")
     ap.add_argument("--kernel", default="auto", choices=["auto", "fused", "split", "vec", "cluster", "hybrid", "band"])
     ap.add_argument("--no-tune", action="store_true", help="skip the launch-configuration autotuner")
     ap.add_argument("--no-extras", action="store_true", help="skip plain path, CPU baseline and kernel profile")
@@ -246,9 +247,10 @@ def run_mine(args):
     from swit_gb300.engine import checkpoint_interval
     ckpt = (checkpoint_interval(sv.nx, sv.nz, sv.npml, sv.nt, per_rank, 0) if args.checkpoint == "auto"
             else int(args.checkpoint))
-    opts = dict(shots_per_batch=args.batch, block_x=args.block_x, kernel=args.kernel, checkpoint_every=ckpt)
+    opts = dict(shots_per_batch=args.batch, block_x=args.block_x, kernel=args.kernel, checkpoint_every=ckpt,
+                graph_branches=args.branches)
     tuned = None
-    if not args.no_tune and args.batch == 0 and args.block_x == 0 and args.kernel == "auto":
+    if not args.no_tune and args.batch == 0 and args.block_x == 0 and args.kernel == "auto" and args.branches == 0:
         from swit_gb300 import autotune
         best, trials = autotune.tune(sv.nx, sv.nz, sv.npml, sv.dx, sv.dt, src_xz, rec_xz, sv.vp_init, rho,
                                      free_surface=sv.free_surface)
@@ -337,7 +339,7 @@ def run_mine(args):
             "config": {"workload": sv.name, "grid": [sv.nx, sv.nz], "npml": sv.npml, "nt": sv.nt,
                        "shots_per_gpu": per_rank, "receivers": sv.ng, "dx_m": sv.dx, "dt_s": sv.dt,
                        "path": "batched, CUDA graph", "kernel": q["kernel"], "shots_per_launch": q["shots_per_batch"],
-                       "block_x": q["block_x"], "parallelism": "shots" + ("" if world == 1 else " x%d ranks" % world),
+                       "block_x": q["block_x"], "graph_branches": q["graph_branches"], "parallelism": "shots" + ("" if world == 1 else " x%d ranks" % world),
                        "l2": "inputs larger than L2: each step streams %.2f GB of boundary strips and %.2f GB of "
                              "traces" % (per_rank * sv.nt * (9 * sv.nx + 6 * sv.nz) * 4 / 1e9,
                                          2 * per_rank * sv.ng * sv.nt * 4 / 1e9)},
@@ -361,7 +363,11 @@ def run_mine(args):
         # per-kernel launch durations (CUDA events around every launch)
         prof = eng.profile_kernels()
         kb = kernel_bytes_per_shot(sv.nx, sv.nz, sv.npml, sv.ng, sv.nt)
-        shots_launch = q["shots_per_batch"]
+        nbatch = -(-per_rank // q["shots_per_batch"])
+        ngroup = -(-nbatch // max(1, q["graph_branches"])) if q["kernel"] == "vec" else nbatch
+        # vec: one timed launch is a group of graph_branches batches launched together on
+        # the graph's concurrent branches (as the captured graphs run them)
+        shots_launch = per_rank / ngroup  # mean shots per timed launch (the last batch may be smaller)
         tot = {k: v["launches"] * v["mean_ms"] for k, v in prof.items()}
         top = max(tot, key=tot.get)
         alg = kb[top] * shots_launch
@@ -371,6 +377,8 @@ def run_mine(args):
                             "frac": achieved / peak, "peak_kind": peak_kind,
                             "traffic": traffic * shots_launch if traffic else None,
                             "algorithmic_bytes_per_launch": alg, "mean_launch_ms": prof[top]["mean_ms"],
+                            "shots_per_launch": shots_launch,
+                            "concurrent_batches_per_launch": q["graph_branches"] if q["kernel"] == "vec" else 1,
                             "kernels": {k: dict(v, share=tot[k] / sum(tot.values())) for k, v in prof.items()}}
         # plain one-shot-per-launch path on a bounded sample
         nplain = min(4, per_rank)

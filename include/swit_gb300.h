@@ -69,7 +69,10 @@ typedef struct swit_desc {
   int32_t path;             /* 0 = batched shots + captured CUDA graph (default),
                                1 = plain: one shot per launch, one launch per
                                kernel and step, no graph                          */
-  int32_t shots_per_batch;  /* batched path: shots per launch, 0 = automatic    */
+  int32_t shots_per_batch;  /* batched path: shots per launch, 0 = automatic
+                               (vec kernels: as many shots in flight as keep the
+                               reverse loop's state in L2, spread evenly over
+                               the graph branches; other kernels: all shots)    */
   int32_t block_x;          /* columns per CTA, 0 = automatic: split kernels
                                1, 2, 4 or 8 (x 32 rows); fused kernels 8, 16
                                or 32 (x all rows); vec kernels: task lists
@@ -101,6 +104,11 @@ typedef struct swit_desc {
                                Same results bit for bit; about one more forward
                                pass of work; export/import of snapshots and
                                swit_profile_kernels need k = 0                 */
+  int32_t graph_branches;   /* batched path: the shot batches' step chains form
+                               this many concurrent branches of the captured
+                               graphs (batch b on branch b mod graph_branches);
+                               0 = automatic (3 with automatic shots_per_batch,
+                               else 2), at most 4                               */
 } swit_desc;
 
 /* Creates an engine and allocates its device workspace on the current device.
@@ -200,9 +208,11 @@ int swit_forward_shot_static(int32_t nx, int32_t nz, int32_t npml, int32_t nt, f
                              const float* rec_z, const float* vp, const float* rho, const float* src, float* seis,
                              void* stream);
 
-/* Sizes the engine has allocated; any pointer may be NULL. */
+/* Sizes and launch configuration the engine has chosen (graph_branches: the
+ * concurrent branches its graphs use); any pointer may be NULL. */
 int swit_query(const swit_engine* e, int64_t* device_bytes, int32_t* shots_per_batch, int32_t* block_x,
-               int32_t* kernels_per_forward, int32_t* kernels_per_backward, int32_t* kernel_variant);
+               int32_t* kernels_per_forward, int32_t* kernels_per_backward, int32_t* kernel_variant,
+               int32_t* graph_branches);
 
 /* Waits for `stream` and reports whether any kernel of the engine gave up
  * waiting for the copies it stages into shared memory (band variant: every such

@@ -26,7 +26,8 @@ class SwitDesc(C.Structure):
                 ("ng_max", C.c_int32), ("ng", C.c_void_p), ("src_x", C.c_void_p), ("src_z", C.c_void_p),
                 ("rec_x", C.c_void_p), ("rec_z", C.c_void_p), ("precision", C.c_int32), ("path", C.c_int32),
                 ("shots_per_batch", C.c_int32), ("block_x", C.c_int32),
-                ("kernel_variant", C.c_int32), ("checkpoint_every", C.c_int32)]
+                ("kernel_variant", C.c_int32), ("checkpoint_every", C.c_int32),
+                ("graph_branches", C.c_int32)]
 
 
 class SwitError(RuntimeError):
@@ -61,7 +62,7 @@ def load(build_if_missing: bool = True):
         "swit_import_snapshot": ([vp, vp, vp, vp, vp, vp, i, vp], i),
         "swit_profile_kernels": ([vp, C.POINTER(C.c_int32), C.POINTER(C.c_double), vp], i),
         "swit_query": ([vp, C.POINTER(C.c_int64), C.POINTER(C.c_int32), C.POINTER(C.c_int32),
-                        C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.POINTER(C.c_int32)], i),
+                        C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.POINTER(C.c_int32)], i),
         "swit_destroy": ([vp], i),
         "swit_check": ([vp, vp], i),
         "swit_misfit_l2": ([vp, vp, vp, C.POINTER(C.c_double), C.c_int32, vp], i),

@@ -2,7 +2,7 @@
 
 Times a short Waveform-gradient run (the full geometry and shot count, a few
 dozen time steps) for each candidate (kernel variant, columns per CTA, shots
-per launch) and returns the fastest.  Every candidate computes bit-identical
+per launch, concurrent graph branches) and returns the fastest.  Every candidate computes bit-identical
 results, so the choice only affects speed.  Results are cached per process
 by problem shape.
 """
@@ -26,10 +26,14 @@ def candidates(ns, nz_pml):
         for tx in (8, 16, 32):
             for b in batches:
                 out.append(dict(kernel="fused", block_x=tx, shots_per_batch=b))
-    vb = sorted({ns, max(1, -(-ns // 2)), max(1, -(-ns // 4)), max(1, -(-ns // 8))}, reverse=True)
-    for bx in (2, 4):
+    # vec: the engine's automatic choice (L2-sized batches on three branches), then
+    # 1..8 batches on 1..4 concurrent graph branches (no more branches than batches)
+    out.append(dict(kernel="vec", block_x=4, shots_per_batch=0, graph_branches=0))
+    vb = sorted({-(-ns // k) for k in range(1, 9)}, reverse=True)
+    for br in (1, 2, 3, 4):
         for b in vb:
-            out.append(dict(kernel="vec", block_x=bx, shots_per_batch=b))
+            if br == 1 or br <= -(-ns // b):
+                out.append(dict(kernel="vec", block_x=4, shots_per_batch=b, graph_branches=br))
     out.append(dict(kernel="split", block_x=4, shots_per_batch=ns))
     out.append(dict(kernel="cluster", block_x=8, shots_per_batch=ns))
     out.append(dict(kernel="hybrid", block_x=8, shots_per_batch=max(1, (ns + 1) // 2)))

@@ -54,7 +54,7 @@ namespace swit {
 void set_last_error(const char* msg) { g_err = msg; }
 }  // namespace swit
 
-constexpr int kCapStreamsMax = 2;  // capture streams per engine (graph branches)
+constexpr int kCapStreamsMax = 4;  // concurrent branches of a captured graph, at most
 
 struct swit_engine {
   // problem
@@ -108,8 +108,9 @@ struct swit_engine {
   bool model_set = false, fwd_ready = false;
   cudaStream_t cap = nullptr;
   // further capture streams: batches run round-robin over the branches of the graphs (capture_fork)
-  cudaStream_t capx[1] = {nullptr};
-  cudaEvent_t ev_fork = nullptr, ev_join[1] = {nullptr};
+  cudaStream_t capx[kCapStreamsMax - 1] = {};
+  cudaEvent_t ev_fork = nullptr, ev_join[kCapStreamsMax - 1] = {};
+  int branches = 2;  // graph branches in use (swit_desc.graph_branches)
   cudaGraphExec_t gfwd[2] = {nullptr, nullptr};
   cudaGraphExec_t gbwd = nullptr;
   int launches_fwd = 0, launches_bwd = 0;
@@ -504,16 +505,20 @@ void backward_checkpointed(swit_engine* e, int s0, int nb, cudaStream_t st) {
 // concurrent branches of the graph; kernels of different branches fill each
 // other's tails and launch gaps.  Batches share no array (each shot owns its
 // wavefields, strips and sums), so the order between them does not matter.
-// Two branches measured best at 481x141 (more branches hold more state than the
-// L2 keeps: 13-shot batches, 125.9 shot-gradients/s with two, 114.5 with four).
-constexpr int kCapStreams = kCapStreamsMax;
-inline cudaStream_t capture_stream(swit_engine* e, int b) { return b % kCapStreams ? e->capx[b % kCapStreams - 1] : e->cap; }
+// What counts is the state of the shots in flight against the L2 and equal work
+// per branch (auto_batches): at 481x141, 127.6 shot-gradients/s with three
+// branches of 9-shot batches, 126.0 with two of 13, 105.3 with 13-shot batches
+// on three branches (one branch runs two batches) and 101.6 with one chain.
+inline cudaStream_t capture_stream(swit_engine* e, int b) {
+  const int k = b % e->branches;
+  return k ? e->capx[k - 1] : e->cap;
+}
 inline void capture_fork(swit_engine* e) {
   cudaEventRecord(e->ev_fork, e->cap);
-  for (int i = 0; i < kCapStreams - 1; ++i) cudaStreamWaitEvent(e->capx[i], e->ev_fork, 0);
+  for (int i = 0; i < e->branches - 1; ++i) cudaStreamWaitEvent(e->capx[i], e->ev_fork, 0);
 }
 inline void capture_join(swit_engine* e) {
-  for (int i = 0; i < kCapStreams - 1; ++i) {
+  for (int i = 0; i < e->branches - 1; ++i) {
     cudaEventRecord(e->ev_join[i], e->capx[i]);
     cudaStreamWaitEvent(e->cap, e->ev_join[i], 0);
   }
@@ -913,9 +918,96 @@ int export_impl(swit_engine* e, void* boundary, void* pend, void* uend, void* we
 }
 
 // Per-launch timing of the stencil kernels with CUDA events.
+// Launch profile of the vec kernels as the graphs run them: the batches of a
+// group of `branches` consecutive batches are launched together on the
+// branches' streams (forked from and joined to `st`), and one timed launch is
+// the whole group, CUDA events on `st` around fork and join.
+template <class R>
+int profile_vec_groups(swit_engine* e, int32_t launches[4], double mean_ms[4], cudaStream_t st) {
+  Grid<R> g = make_grid<R>(e);
+  const int B = e->batch, nbatch = (e->ns + B - 1) / B;
+  const int br = std::min(e->branches, nbatch);
+  std::vector<cudaEvent_t> ev[4];
+  auto record = [&](int which) {
+    cudaEvent_t a;
+    cudaEventCreate(&a);
+    ev[which].push_back(a);
+    cudaEventRecord(a, st);
+  };
+  auto fork = [&](int gn) {
+    cudaEventRecord(e->ev_fork, st);
+    for (int i = 0; i < gn - 1; ++i) cudaStreamWaitEvent(e->capx[i], e->ev_fork, 0);
+  };
+  auto join = [&](int gn) {
+    for (int i = 0; i < gn - 1; ++i) {
+      cudaEventRecord(e->ev_join[i], e->capx[i]);
+      cudaStreamWaitEvent(st, e->ev_join[i], 0);
+    }
+  };
+  auto group = [&](int which, int b0, int gn, int it) {
+    record(which);
+    fork(gn);
+    for (int j = 0; j < gn; ++j) {
+      const int s0 = (b0 + j) * B, nb = std::min(B, e->ns - s0);
+      cudaStream_t cs = j ? e->capx[j - 1] : st;
+      if (which == 0)
+        k_fwd_p_v<R><<<vec_grid(e, 0, nb), vec_block(e), 0, cs>>>(g, vec_list(e, 0), make_src(e), (const R*)e->src,
+                                                                (R*)e->p, (const R*)e->u, (const R*)e->w, it, s0);
+      else if (which == 1)
+        k_fwd_uw_v<R><<<vec_grid(e, 1, nb), vec_block(e), 0, cs>>>(g, vec_list(e, 1), make_rec(e), (const R*)e->p,
+                                                                 (R*)e->u, (R*)e->w, (R*)e->seis_t,
+                                                                 (R*)e->strips, it, s0);
+      else if (which == 2)
+        k_bwd_uw_v<R><<<vec_grid(e, 2, nb), vec_block(e), 0, cs>>>(g, vec_list(e, 2), (const R*)e->pb, (R*)e->ub,
+                                                                 (R*)e->wb, (const R*)e->pe, (R*)e->ue, (R*)e->we,
+                                                                 (const R*)e->strips, it, s0);
+      else
+        k_bwd_p_v<R><<<vec_grid(e, 3, nb), vec_block(e), 0, cs>>>(
+            g, vec_list(e, 3), make_rec(e), make_src(e), (const R*)e->src, (const R*)e->adj_t, (R*)e->pb,
+            (const R*)e->ub, (const R*)e->wb, (R*)e->pe, (const R*)e->ue, (const R*)e->we, (R*)e->dg, (R*)e->dfw,
+            (R*)e->dbk, (const R*)e->strips, it, s0);
+    }
+    join(gn);
+    record(which);
+  };
+  const size_t fb = (size_t)e->ns * g.FSZ * e->esz, ib = (size_t)e->ns * g.FSI * e->esz;
+  for (void* q : {e->p, e->u, e->w}) CK(cudaMemsetAsync(q, 0, fb, st));
+  for (int b0 = 0; b0 < nbatch; b0 += br)
+    for (int it = 2; it <= e->nt; ++it) {
+      group(0, b0, std::min(br, nbatch - b0), it);
+      group(1, b0, std::min(br, nbatch - b0), it);
+    }
+  for (void* q : {e->pb, e->ub, e->wb}) CK(cudaMemsetAsync(q, 0, fb, st));
+  CK(cudaMemsetAsync(e->dg, 0, ib, st));
+  CK(cudaMemsetAsync(e->dfw, 0, ib, st));
+  CK(cudaMemsetAsync(e->dbk, 0, ib, st));
+  copy_end<R>(e, st);
+  for (int b0 = 0; b0 < nbatch; b0 += br)
+    for (int it = e->nt; it >= 2; --it) {
+      group(2, b0, std::min(br, nbatch - b0), it);
+      group(3, b0, std::min(br, nbatch - b0), it);
+    }
+  CK(cudaGetLastError());
+  CK(cudaStreamSynchronize(st));
+  for (int q = 0; q < 4; ++q) {
+    double tot = 0.0;
+    const size_t n = ev[q].size() / 2;
+    for (size_t i = 0; i < n; ++i) {
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, ev[q][2 * i], ev[q][2 * i + 1]);
+      tot += ms;
+    }
+    for (cudaEvent_t x : ev[q]) cudaEventDestroy(x);
+    launches[q] = (int32_t)n;
+    mean_ms[q] = n ? tot / n : 0.0;
+  }
+  return 0;
+}
+
 template <class R>
 int profile_impl(swit_engine* e, int32_t launches[4], double mean_ms[4], cudaStream_t st) {
   if (e->ckpt_k) return fail(SWIT_E_STATE, "this call needs boundary saving (checkpoint_every = 0)");
+  if (e->variant == 3 && e->path == 0) return profile_vec_groups<R>(e, launches, mean_ms, st);
   Grid<R> g = make_grid<R>(e);
   const int nshot_launch = e->path == 1 ? 1 : e->batch;
   std::vector<cudaEvent_t> ev[4];
@@ -1453,6 +1545,30 @@ extern "C" {
 
 const char* swit_last_error(void) { return g_err.c_str(); }
 
+// Automatic shots per launch and graph branches of the vec kernels.  The
+// reverse loop touches per shot 3 wavefields on the PML grid and 6 interior
+// arrays; the step kernels are fastest when the shots of the branches in flight
+// keep that state in L2 (about 0.7 of it, the rest holding strips, traces and
+// coefficients) and when the branches carry equal work.  So: shots in flight T =
+// 0.7 L2 / state, branches br (3 unless given), batches k = br * ceil(ns / T)
+// (a multiple of br, so the branches get the same number of launches) and
+// ceil(ns / k) shots per batch.  At 481x141 (npml 40) on GB300: 28 shots in
+// flight, 6 batches of 9 on 3 branches.
+void auto_batches(swit_engine* e, int branches) {
+  int dev = 0, l2 = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, dev) != cudaSuccess ||
+      l2 <= 0)
+    l2 = 64 << 20;
+  const double state = (3.0 * e->NX * e->NZ + 6.0 * e->nx * e->nz) * e->esz;
+  const int inflight = std::max(1, (int)(0.7 * l2 / state));
+  const int br = std::max(1, std::min(branches ? branches : 3, e->ns));
+  const int per_branch = std::max(1, inflight / br);
+  const int rounds = (e->ns + br * per_branch - 1) / (br * per_branch);
+  const int k = std::min(e->ns, br * rounds);
+  e->batch = (e->ns + k - 1) / k;
+  e->branches = br;
+}
+
 int swit_create(const swit_desc* d, swit_engine** out) {
   if (!d || !out) return fail(SWIT_E_ARG, "null argument");
   *out = nullptr;
@@ -1537,6 +1653,13 @@ int swit_create(const swit_desc* d, swit_engine** out) {
     return fail(SWIT_E_ARG, "checkpointed recomputation needs the vec or band kernels (kernel_variant 0, 3 or 6)");
   }
   e->ckpt_k = std::min(d->checkpoint_every, e->nt);
+  if (d->graph_branches < 0 || d->graph_branches > kCapStreamsMax) {
+    delete e;
+    return fail(SWIT_E_ARG, "graph_branches must be 0 (automatic) or 1..%d (got %d)", kCapStreamsMax,
+                d->graph_branches);
+  }
+  e->branches = d->graph_branches ? d->graph_branches : 2;
+  if (d->shots_per_batch == 0 && e->path == 0 && e->variant == 3) auto_batches(e, d->graph_branches);
   e->ckpt_m = e->ckpt_k ? (e->nt + e->ckpt_k - 1) / e->ckpt_k : 0;
   e->snt = e->ckpt_k ? e->ckpt_k : e->nt;
   e->sit0 = 1;
@@ -1803,8 +1926,10 @@ int swit_profile_kernels(swit_engine* e, int32_t launches[4], double mean_ms[4],
 }
 
 int swit_query(const swit_engine* e, int64_t* device_bytes, int32_t* shots_per_batch, int32_t* block_x,
-               int32_t* kernels_per_forward, int32_t* kernels_per_backward, int32_t* kernel_variant) {
+               int32_t* kernels_per_forward, int32_t* kernels_per_backward, int32_t* kernel_variant,
+               int32_t* graph_branches) {
   if (!e) return fail(SWIT_E_ARG, "null argument");
+  if (graph_branches) *graph_branches = e->path == 1 ? 1 : std::min(e->branches, (e->ns + e->batch - 1) / e->batch);
   if (device_bytes) *device_bytes = (int64_t)e->bytes;
   if (shots_per_batch) *shots_per_batch = e->path == 1 ? 1 : e->batch;
   if (block_x) *block_x = e->bx;

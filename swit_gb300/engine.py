@@ -27,7 +27,8 @@ class Engine:
     """
 
     def __init__(self, nx, nz, npml, nt, dx, dt, src_xz, rec_xz, free_surface=1, ng=None, precision="fp32",
-                 path="batched", shots_per_batch=0, block_x=0, kernel="auto", checkpoint_every=0, _borrow=None):
+                 path="batched", shots_per_batch=0, block_x=0, kernel="auto", checkpoint_every=0, graph_branches=0,
+                 _borrow=None):
         lib = _lib.load()
         src_xz = np.asarray(src_xz, dtype=np.float32).reshape(-1, 2)
         rec_xz = np.asarray(rec_xz, dtype=np.float32)
@@ -57,7 +58,7 @@ class Engine:
                           self.ngmax, k["ng"].ctypes.data, k["xs"].ctypes.data, k["zs"].ctypes.data,
                           k["xg"].ctypes.data, k["zg"].ctypes.data, 1 if self.fp64 else 0,
                           1 if path == "plain" else 0, int(shots_per_batch), int(block_x), variants[kernel],
-                          int(checkpoint_every))
+                          int(checkpoint_every), int(graph_branches))
         self.checkpoint_every = int(checkpoint_every)
         self._desc = d
         self._lib = lib
@@ -207,10 +208,11 @@ class Engine:
 
     def query(self):
         by = C.c_int64()
-        sb, bx, kf, kb, kv = C.c_int32(), C.c_int32(), C.c_int32(), C.c_int32(), C.c_int32()
+        sb, bx, kf, kb, kv, br = C.c_int32(), C.c_int32(), C.c_int32(), C.c_int32(), C.c_int32(), C.c_int32()
         _lib.check(self._lib.swit_query(self._h, C.byref(by), C.byref(sb), C.byref(bx), C.byref(kf), C.byref(kb),
-                                        C.byref(kv)))
-        return dict(device_bytes=by.value, shots_per_batch=sb.value, block_x=bx.value, kernels_per_forward=kf.value,
+                                        C.byref(kv), C.byref(br)))
+        return dict(device_bytes=by.value, shots_per_batch=sb.value, block_x=bx.value, graph_branches=br.value,
+                    kernels_per_forward=kf.value,
                     kernels_per_backward=kb.value, kernel={1: "split", 2: "fused", 3: "vec", 4: "cluster", 5: "hybrid", 6: "band"}.get(kv.value, "?"))
 
     def check(self):

@@ -48,6 +48,7 @@ def _desc(s, **over):
     (dict(block_x=3, kernel_variant=1), _lib.SwitError), (dict(block_x=12, kernel_variant=2), _lib.SwitError),
     (dict(kernel_variant=7), _lib.SwitError), (dict(checkpoint_every=-1), _lib.SwitError),
     (dict(checkpoint_every=5, kernel_variant=1), _lib.SwitError),
+    (dict(graph_branches=-1), _lib.SwitError), (dict(graph_branches=5), _lib.SwitError),
 ])
 def test_create_rejects_bad_descriptions_before_any_gpu_work(over, code):
     lib = _lib.load()

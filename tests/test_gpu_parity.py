@@ -108,7 +108,12 @@ def test_gradient_l2_single_call_matches_oracle(base):
                                   dict(kernel="hybrid", block_x=3, shots_per_batch=2),
                                   dict(kernel="hybrid", path="plain"), dict(kernel="band"),
                                   dict(kernel="band", block_x=1), dict(kernel="band", block_x=3),
-                                  dict(kernel="band", block_x=7, shots_per_batch=2), dict(kernel="band", path="plain")])
+                                  dict(kernel="band", block_x=7, shots_per_batch=2), dict(kernel="band", path="plain"),
+                                  dict(kernel="vec", shots_per_batch=1, graph_branches=1),
+                                  dict(kernel="vec", shots_per_batch=1, graph_branches=3),
+                                  dict(kernel="vec", shots_per_batch=1, graph_branches=4),
+                                  dict(kernel="split", shots_per_batch=1, graph_branches=3),
+                                  dict(kernel="band", shots_per_batch=1, graph_branches=4)])
 def test_launch_variants_are_identical(base, opts):
     s = base["s"]
     with engine(s, **opts) as e:
@@ -273,6 +278,7 @@ def test_cluster_variant_rejects_a_grid_that_does_not_fit_on_chip():
 @pytest.mark.parametrize("opts", [dict(checkpoint_every=1), dict(checkpoint_every=7), dict(checkpoint_every=64),
                                   dict(checkpoint_every=298), dict(checkpoint_every=299),
                                   dict(checkpoint_every=1000), dict(checkpoint_every=13, shots_per_batch=2),
+                                  dict(checkpoint_every=13, shots_per_batch=1, graph_branches=3),
                                   dict(checkpoint_every=13, path="plain"), dict(checkpoint_every=13, kernel="band")])
 def test_checkpointed_recomputation_gives_the_boundary_saving_results(base, opts):
     """Checkpoints every k steps instead of strips; the reverse loop re-runs each
@@ -303,3 +309,27 @@ def test_checkpointed_gradient_l2_and_snapshot_refusal(base):
     for k in ("grad", "illum_fw", "illum_bk"):
         np.testing.assert_array_equal(r[k], r0[k])
     assert r["misfit"] == r0["misfit"]
+
+
+@pytest.mark.parametrize("opts,groups", [(dict(kernel="vec", shots_per_batch=1, graph_branches=2), 2),
+                                         (dict(kernel="vec", shots_per_batch=1, graph_branches=3), 1),
+                                         (dict(kernel="vec", shots_per_batch=1, graph_branches=1), 3),
+                                         (dict(kernel="split"), 1)])
+def test_kernel_profile_counts_launches_and_leaves_results_intact(base, opts, groups):
+    """swit_profile_kernels times every step launch (vec: each group of batches
+    launched together on the graph's branches); the engine still computes the
+    oracle's gradient afterwards."""
+    s = base["s"]
+    assert s.ns == 3
+    with engine(s, **opts) as e:
+        e.set_model(s.vp_true, base["rho"])
+        e.forward(base["src"], save_boundary=True)
+        e.backward(base["adj"])
+        prof = e.profile_kernels()
+        seis = e.forward(base["src"], save_boundary=True)
+        g, fw, bk = e.backward(base["adj"])
+    for k, v in prof.items():
+        assert v["launches"] == groups * (s.nt - 1), k
+        assert v["mean_ms"] > 0, k
+    np.testing.assert_array_equal(seis, base["ref"]["seis"])
+    np.testing.assert_array_equal(g, base["grad"]["g"])
