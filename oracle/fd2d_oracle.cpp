@@ -163,7 +163,7 @@ struct Setup {
 // reference's boundary(S, nt) layout (S fastest); csg in [ig][it] layout.
 template <class R>
 void forward_shot(const Setup<R>& S, const oracle_desc& d, int is, const float* s_in, bool store,
-                  R* seis, R* boundary, R* p_end, R* u_end, R* w_end) {
+                  R* seis, R* boundary, R* p_end, R* u_end, R* w_end, R* dsave = nullptr) {
   const int NX = S.NX, NZ = S.NZ, npml = S.npml, nt = S.nt, nx = S.nx, nz = S.nz;
   const R dt = S.dt, dx = S.dx, c1 = S.c1, c2 = S.c2;
   const int SL = strip_len(nx, nz);
@@ -192,9 +192,11 @@ void forward_shot(const Setup<R>& S, const oracle_desc& d, int is, const float* 
       for (int iz = fs[ix] + 1; iz <= NZ - 2; ++iz) {
         R alpha = S.den(iz, ix) * S.c(iz, ix) * S.c(iz, ix) * dt / dx;
         R kappa = S.damp_g(iz, ix) * dt;
-        p(iz, ix) = (R(1.0) - kappa) * p(iz, ix) -
-                    alpha * (c1 * (u(iz, ix) - u(iz, ix - 1) + w(iz, ix) - w(iz - 1, ix)) +
-                             c2 * (u(iz, ix + 1) - u(iz, ix - 2) + w(iz + 1, ix) - w(iz - 2, ix)));
+        // the divergence term D; the exact adjoint reads it back (dsave)
+        const R D = c1 * (u(iz, ix) - u(iz, ix - 1) + w(iz, ix) - w(iz - 1, ix)) +
+                    c2 * (u(iz, ix + 1) - u(iz, ix - 2) + w(iz + 1, ix) - w(iz - 2, ix));
+        p(iz, ix) = (R(1.0) - kappa) * p(iz, ix) - alpha * D;
+        if (dsave) dsave[((size_t)(it - 1) * NX + (ix - 1)) * NZ + (iz - 1)] = D;
       }
     // source, fdcore.f90:88-89
     p(isz, isx) = p(isz, isx) + dt * s[it];
@@ -596,6 +598,159 @@ int gradient_all(const oracle_desc* d, const float* vp, const float* rho, const 
   return 0;
 }
 
+// ---------------------------------------------------------------------------
+// Exact discrete adjoint of forward_shot (not a reference algorithm: the
+// transpose of the reference's FP forward recursion, fdcore.f90:75-128, for the
+// vp gradient and the source gradient).  With the damping held fixed (vmin and
+// so the damping profile are treated as constants), step it maps (p, u, w) by
+//   S1  p := (1-kp) p - A D(u, w)       on ix in [3,NX-2], iz in [fs+1,NZ-2]
+//   S2  p(isz,isx) += dt s(it)
+//   S3  p(fs-1,:) := -p(fs+1,:)         (free surface)
+//   S4  u := (1-ku) u - B Gx(p)         on ix in [2,NX-2], iz in [fs,NZ-1]
+//       w := (1-kw) w - B Gz(p)         on ix in [2,NX-1], iz in [fs,NZ-2]
+//   S5  w(fs-1,:) := w(fs,:)            (free surface)
+//   S6  seis(ig, it) = p(gz, gx)
+// with A = den c^2 dt/dx, B = dt/(den dx).  The adjoint runs it = nt..2 in two
+// gather passes per step (the form the GB300 kernels take, so both evaluate the
+// same expressions in the same order):
+//   K1 (pressure points of S1's range): lp = (1-kp) lp [S1 scaling of step it+1]
+//      + adjoint sources [S6] + the S4 transposes from lu, lw~ [w~(fs) = w(fs) +
+//      m, the S5 fold] - c2 B(fs) w~(fs) at row fs+1 [S3 fold]; the source
+//      gradient dt lp [S2]; gA -= lp D_it [S1]; p := lp (unscaled).
+//   K2 (velocity points): lu = (1-ku) lu + S1 transposes from lp; likewise lw
+//      from lw~; m_new(ix) = c2 A(fs+1,ix) lp(fs+1,ix) [S1's read of w(fs-1)].
+// m alternates between two rows by step parity.  gA is the gradient with respect
+// to A per PML point; dJ/dc = gA 2 den c dt/dx, and dJ/dvp sums dJ/dc over the
+// PML points padded from each interior point (io.f90:243-292: clamp to the
+// interior).  dsave holds D of every step: [it-1][ix-1][iz-1].
+template <class R>
+void exact_adjoint_shot(const Setup<R>& S, const oracle_desc& d, int is, const float* sadj_in, const R* dsave,
+                        R* gA, R* gsrc) {
+  const int NX = S.NX, NZ = S.NZ, nt = S.nt;
+  const R dt = S.dt, dx = S.dx, c1 = S.c1, c2 = S.c2;
+  const auto& fs = S.fs;
+  const int F = fs[1];  // flat free surface
+  const bool fold = S.fs_flag == 1;
+  F2<R> A, B, kp, ku, kw, lp, lu, lw;
+  for (F2<R>* a : {&A, &B, &kp, &ku, &kw, &lp, &lu, &lw}) a->init(NZ, NX);
+  for (int ix = 1; ix <= NX; ++ix)
+    for (int iz = 1; iz <= NZ; ++iz) {
+      A(iz, ix) = S.den(iz, ix) * S.c(iz, ix) * S.c(iz, ix) * dt / dx;
+      B(iz, ix) = dt / (S.den(iz, ix) * dx);
+      kp(iz, ix) = S.damp_g(iz, ix) * dt;
+      if (ix + 1 <= NX) ku(iz, ix) = R(0.5) * (S.damp_g(iz, ix) + S.damp_g(iz, ix + 1)) * dt;
+      if (iz + 1 <= NZ) kw(iz, ix) = R(0.5) * (S.damp_g(iz, ix) + S.damp_g(iz + 1, ix)) * dt;
+    }
+  std::vector<R> m[2] = {std::vector<R>(NX + 1, R(0)), std::vector<R>(NX + 1, R(0))};
+  int isx = S.gidx(d.xs[is]);
+  int isz = S.gidx(d.zs[is]);
+  if (isz == fs[isx]) isz = isz + 1;
+  const int ng = d.ng[is];
+  std::vector<int> gx(ng), gz(ng);
+  for (int ig = 0; ig < ng; ++ig) {
+    gx[ig] = S.gidx(d.xg[(size_t)is * d.ngmax + ig]);
+    gz[ig] = S.gidx(d.zg[(size_t)is * d.ngmax + ig]);
+    if (gz[ig] == fs[gx[ig]]) gz[ig] = gz[ig] + 1;
+  }
+  auto inRp = [&](int iz, int ix) { return ix >= 3 && ix <= NX - 2 && iz >= F + 1 && iz <= NZ - 2; };
+  for (int it = 1; it <= nt; ++it) gsrc[it - 1] = R(0);
+  for (int it = nt; it >= 2; --it) {
+    const std::vector<R>& mo = m[it & 1];
+    std::vector<R>& mn = m[(it - 1) & 1];
+    auto wt = [&](int iz, int ix) -> R { return (fold && iz == F) ? lw(iz, ix) + mo[ix] : lw(iz, ix); };
+    const R* D = dsave + (size_t)(it - 1) * NX * NZ;
+    // K1
+    for (int ix = 3; ix <= NX - 2; ++ix)
+      for (int iz = F + 1; iz <= NZ - 2; ++iz) {
+        R l = (R(1.0) - kp(iz, ix)) * lp(iz, ix);
+        for (int ig = 0; ig < ng; ++ig)
+          if (gz[ig] == iz && gx[ig] == ix) l = l + (R)sadj_in[(size_t)ig * nt + (it - 1)];
+        l = l - c1 * (B(iz, ix - 1) * lu(iz, ix - 1));
+        l = l + c1 * (B(iz, ix) * lu(iz, ix));
+        if (ix - 2 >= 2) l = l - c2 * (B(iz, ix - 2) * lu(iz, ix - 2));
+        if (ix + 1 <= NX - 2) l = l + c2 * (B(iz, ix + 1) * lu(iz, ix + 1));
+        l = l - c1 * (B(iz - 1, ix) * wt(iz - 1, ix));
+        l = l + c1 * (B(iz, ix) * wt(iz, ix));
+        if (iz - 2 >= F) l = l - c2 * (B(iz - 2, ix) * wt(iz - 2, ix));
+        if (iz + 1 <= NZ - 2) l = l + c2 * (B(iz + 1, ix) * wt(iz + 1, ix));
+        if (fold && iz == F + 1) l = l - c2 * (B(F, ix) * wt(F, ix));
+        if (iz == isz && ix == isx) gsrc[it - 1] = dt * l;
+        const size_t k = (size_t)(ix - 1) * NZ + (iz - 1);
+        gA[k] = gA[k] - l * D[k];
+        lp(iz, ix) = l;
+      }
+    // K2 (reads lp from K1, m[it&1]; writes lu, lw, m[(it-1)&1])
+    for (int ix = 2; ix <= NX - 1; ++ix)
+      for (int iz = F; iz <= NZ - 1; ++iz) {
+        if (ix <= NX - 2) {
+          R l = (R(1.0) - ku(iz, ix)) * lu(iz, ix);
+          if (inRp(iz, ix)) l = l - c1 * (A(iz, ix) * lp(iz, ix));
+          if (inRp(iz, ix + 1)) l = l + c1 * (A(iz, ix + 1) * lp(iz, ix + 1));
+          if (inRp(iz, ix - 1)) l = l - c2 * (A(iz, ix - 1) * lp(iz, ix - 1));
+          if (inRp(iz, ix + 2)) l = l + c2 * (A(iz, ix + 2) * lp(iz, ix + 2));
+          lu(iz, ix) = l;
+        }
+        if (iz <= NZ - 2) {
+          R l = (R(1.0) - kw(iz, ix)) * wt(iz, ix);
+          if (inRp(iz, ix)) l = l - c1 * (A(iz, ix) * lp(iz, ix));
+          if (inRp(iz + 1, ix)) l = l + c1 * (A(iz + 1, ix) * lp(iz + 1, ix));
+          if (inRp(iz - 1, ix)) l = l - c2 * (A(iz - 1, ix) * lp(iz - 1, ix));
+          if (inRp(iz + 2, ix)) l = l + c2 * (A(iz + 2, ix) * lp(iz + 2, ix));
+          if (fold && iz == F && inRp(F + 1, ix)) mn[ix] = c2 * (A(F + 1, ix) * lp(F + 1, ix));
+          lw(iz, ix) = l;
+        }
+      }
+  }
+}
+
+// dJ/dvp on the interior (nx, nz) from the per-shot gA sums: shots summed in
+// order per PML point, times dA/dc = 2 den c dt/dx, then summed over the PML
+// points each interior point was padded to (columns, then rows ascending).
+template <class R>
+void exact_reduce(const Setup<R>& S, int ns, const std::vector<R>& gA, R* g) {
+  const int NX = S.NX, NZ = S.NZ, L = S.npml, nx = S.nx, nz = S.nz;
+  const size_t N = (size_t)NX * NZ;
+  for (int j = 1; j <= nx; ++j)
+    for (int i = 1; i <= nz; ++i) {
+      const int x0 = j == 1 ? 1 : L + j, x1 = j == nx ? NX : L + j;
+      const int z0 = i == 1 ? 1 : L + i, z1 = i == nz ? NZ : L + i;
+      R acc = R(0);
+      for (int ix = x0; ix <= x1; ++ix)
+        for (int iz = z0; iz <= z1; ++iz) {
+          const size_t k = (size_t)(ix - 1) * NZ + (iz - 1);
+          R t = gA[k];
+          for (int is = 1; is < ns; ++is) t = t + gA[is * N + k];
+          const R dadc = R(2.0) * S.den(iz, ix) * S.c(iz, ix) * S.dt / S.dx;
+          acc = acc + t * dadc;
+        }
+      g[(size_t)(j - 1) * nz + (i - 1)] = acc;
+    }
+}
+
+// Forward of every shot (seismograms, D of every step) and the exact adjoint of
+// adjoint sources adj (ns, ngmax, nt): g = dJ/dvp (nx, nz), gsrc = dJ/dsrc (ns, nt).
+template <class R>
+int exact_all(const oracle_desc* d, const float* vp, const float* rho, const float* src, const float* adj, R* g,
+              R* gsrc, R* seis_out, int nthreads) {
+  int rc = check_desc(d);
+  if (rc) return rc;
+  Setup<R> S;
+  S.build(*d, vp, rho);
+  const size_t N = (size_t)S.NX * S.NZ, NS = (size_t)d->ngmax * d->nt;
+  std::vector<R> gA(d->ns * N, R(0));
+  run_ranks(d->ns, nthreads, [&](int is) {
+    std::vector<R> seis(NS, R(0)), D((size_t)d->nt * N, R(0));
+    forward_shot<R>(S, *d, is, src + (size_t)is * d->nt, false, seis.data(), nullptr, nullptr, nullptr, nullptr,
+                    D.data());
+    if (seis_out)
+      for (size_t k = 0; k < NS; ++k) seis_out[is * NS + k] = seis[k];
+    exact_adjoint_shot<R>(S, *d, is, adj + (size_t)is * NS, D.data(), gA.data() + is * N,
+                          gsrc + (size_t)is * d->nt);
+  });
+  exact_reduce(S, d->ns, gA, g);
+  return 0;
+}
+
 }  // namespace
 
 extern "C" {
@@ -638,6 +793,15 @@ int oracle_gradient_f32(const oracle_desc* d, const float* vp, const float* rho,
 int oracle_gradient_f64(const oracle_desc* d, const float* vp, const float* rho, const float* src, const float* obs,
                         double* g, double* fw, double* bk, double* seis, int nthreads) {
   return gradient_all<double>(d, vp, rho, src, obs, g, fw, bk, seis, nthreads);
+}
+
+int oracle_exact_f32(const oracle_desc* d, const float* vp, const float* rho, const float* src, const float* adj,
+                     float* g, float* gsrc, float* seis, int nthreads) {
+  return exact_all<float>(d, vp, rho, src, adj, g, gsrc, seis, nthreads);
+}
+int oracle_exact_f64(const oracle_desc* d, const float* vp, const float* rho, const float* src, const float* adj,
+                     double* g, double* gsrc, double* seis, int nthreads) {
+  return exact_all<double>(d, vp, rho, src, adj, g, gsrc, seis, nthreads);
 }
 
 }  // extern "C"

@@ -4,7 +4,9 @@ Only tests/, ``__graft_entry__.smoke()`` and bench.py's CPU-baseline leg import
 this module.  It wraps ``libfd2d_oracle.so`` (built by ``oracle/build.py``), a
 statement-by-statement C++ restatement of fd2dmpi's forward
 (fd2dmpi/fdcore.f90:30-198), reconstruction (fdcore.f90:202-289), adjoint
-(fdcore.f90:293-375) and imaging/shot-sum (fd2dmpi/solver.f90:230-270).
+(fdcore.f90:293-375) and imaging/shot-sum (fd2dmpi/solver.f90:230-270), plus
+the exact discrete adjoint of that forward (``exact``; pinned by
+``oracle/exact.py``).
 
 Array conventions (all z-fastest, as SWIT's Python side):
   vp, rho            (nx, nz) float32
@@ -147,6 +149,25 @@ def gradient(pb: Problem, vp, rho, src, obs, fp64=False, return_seis=False, nthr
     if return_seis:
         out["seis"] = seis
     return out
+
+
+def exact(pb: Problem, vp, rho, src, adj, fp64=False, nthreads=None):
+    """Exact discrete adjoint of the forward map (oracle_exact_*): the forward
+    of every shot, then the transpose of its recursion for adjoint sources adj
+    (ns, ngmax, nt).  Returns dict(g = dJ/dvp (nx, nz), gsrc = dJ/dsrc (ns, nt),
+    seis)."""
+    nthreads = nthreads or os.cpu_count()
+    R = np.float64 if fp64 else np.float32
+    ct = C.c_double if fp64 else C.c_float
+    g = np.zeros((pb.nx, pb.nz), R)
+    gsrc = np.zeros((pb.ns, pb.nt), R)
+    seis = np.zeros((pb.ns, pb.ngmax, pb.nt), R)
+    fn = lib().oracle_exact_f64 if fp64 else lib().oracle_exact_f32
+    vp, rho, src, adj = _f32(vp), _f32(rho), _f32(src), _f32(adj)
+    d = pb.desc()
+    rc = fn(C.byref(d), _p(vp), _p(rho), _p(src), _p(adj), _p(g, ct), _p(gsrc, ct), _p(seis, ct), C.c_int(nthreads))
+    _check(rc, "exact")
+    return dict(g=g, gsrc=gsrc, seis=seis)
 
 
 def damp_profile(pb: Problem, vp, rho):
