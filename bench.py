@@ -44,6 +44,8 @@ def parse():
     ap.add_argument("--batch", type=int, default=0, help="shots per launch (0 = engine default)")
     ap.add_argument("--block-x", type=int, default=0)
     ap.add_argument("--branches", type=int, default=0, help="concurrent graph branches (0 = engine default)")
+    ap.add_argument("--adjoint", default="fd2dmpi", choices=["fd2dmpi", "exact"],
+                    help="fd2dmpi's adjoint (the reference's gradient) or the exact discrete adjoint")
     ap.add_argument("--kernel", default="auto", choices=["auto", "fused", "split", "vec", "cluster", "hybrid", "band"])
     ap.add_argument("--no-tune", action="store_true", help="skip the launch-configuration autotuner")
     ap.add_argument("--no-extras", action="store_true", help="skip plain path, CPU baseline and kernel profile")
@@ -236,6 +238,9 @@ def run_mine(args):
     large = args.workload == "large"
     if large:  # no autotune (each trial engine would hold the full survey) and no CPU-side extras
         args.no_tune = args.no_extras = True
+    exact = args.adjoint == "exact"
+    if exact:  # the kernel profile, plain path and CPU baseline time fd2dmpi's adjoint
+        args.no_extras = True
     per_rank = args.shots or (200 if large else 49)
     full = survey.config(3 if large else 1, ns=per_rank * world, nt=args.nt)
     # rank r owns a contiguous block of shots (fd2dmpi/mmi_mpi.f90:52-80)
@@ -248,12 +253,12 @@ def run_mine(args):
     ckpt = (checkpoint_interval(sv.nx, sv.nz, sv.npml, sv.nt, per_rank, 0) if args.checkpoint == "auto"
             else int(args.checkpoint))
     opts = dict(shots_per_batch=args.batch, block_x=args.block_x, kernel=args.kernel, checkpoint_every=ckpt,
-                graph_branches=args.branches)
+                graph_branches=args.branches, adjoint=args.adjoint)
     tuned = None
     if not args.no_tune and args.batch == 0 and args.block_x == 0 and args.kernel == "auto" and args.branches == 0:
         from swit_gb300 import autotune
         best, trials = autotune.tune(sv.nx, sv.nz, sv.npml, sv.dx, sv.dt, src_xz, rec_xz, sv.vp_init, rho,
-                                     free_surface=sv.free_surface)
+                                     free_surface=sv.free_surface, adjoint=args.adjoint)
         opts.update(best)
         tuned = [dict(c, ms=round(t * 1e3, 3)) for c, t in trials]
     eng = Engine(sv.nx, sv.nz, sv.npml, sv.nt, sv.dx, sv.dt, src_xz, rec_xz, **opts)
@@ -267,7 +272,7 @@ def run_mine(args):
 
     def step_device():
         out = eng.gradient_l2(src_d, obs_d)
-        shots.allreduce_sum([out["grad"], out["illum_fw"], out["illum_bk"]])
+        shots.allreduce_sum([out[k] for k in ("grad", "illum_fw", "illum_bk") if out[k] is not None])
         return out
 
     for _ in range(args.warmup):
@@ -306,7 +311,8 @@ def run_mine(args):
         eng.set_model(vp_h, rho_h)
         out = eng.gradient_l2(src_h, obs_h)
         if world > 1:
-            g = torch.from_numpy(np.stack([out["grad"], out["illum_fw"], out["illum_bk"]])).cuda()
+            g = torch.from_numpy(np.stack([out[k] for k in ("grad", "illum_fw", "illum_bk")
+                                           if out[k] is not None])).cuda()
             shots.allreduce_sum([g])
             g.cpu()
         return out
@@ -329,7 +335,7 @@ def run_mine(args):
     LDI = ((sv.nz + 31) // 32) * 32
     h2d = (2 * sv.nx * sv.nz * 4 + src.nbytes + obs_h.numel() * 4 + 2 * NX * LD * 4 + sv.nx * LDI * 4
            + (sv.npml + 1) * 4)
-    d2h = 3 * sv.nx * sv.nz * 4 + per_rank * sv.ng * 8
+    d2h = (1 if exact else 3) * sv.nx * sv.nz * 4 + per_rank * sv.ng * 8
 
     U, B = work_units(sv.nx, sv.nz, sv.npml, sv.nt, sv.ng)
     peak, peak_kind = measured_peak()
@@ -339,7 +345,7 @@ def run_mine(args):
             "config": {"workload": sv.name, "grid": [sv.nx, sv.nz], "npml": sv.npml, "nt": sv.nt,
                        "shots_per_gpu": per_rank, "receivers": sv.ng, "dx_m": sv.dx, "dt_s": sv.dt,
                        "path": "batched, CUDA graph", "kernel": q["kernel"], "shots_per_launch": q["shots_per_batch"],
-                       "block_x": q["block_x"], "graph_branches": q["graph_branches"], "parallelism": "shots" + ("" if world == 1 else " x%d ranks" % world),
+                       "block_x": q["block_x"], "graph_branches": q["graph_branches"], "adjoint": args.adjoint, "parallelism": "shots" + ("" if world == 1 else " x%d ranks" % world),
                        "l2": "inputs larger than L2: each step streams %.2f GB of boundary strips and %.2f GB of "
                              "traces" % (per_rank * sv.nt * (9 * sv.nx + 6 * sv.nz) * 4 / 1e9,
                                          2 * per_rank * sv.ng * sv.nt * 4 / 1e9)},

@@ -109,6 +109,13 @@ typedef struct swit_desc {
                                graphs (batch b on branch b mod graph_branches);
                                0 = automatic (3 with automatic shots_per_batch,
                                else 2), at most 4                               */
+  int32_t adjoint_mode;     /* 0 = fd2dmpi's adjoint (boundary strips, reverse
+                               reconstruction, continuous-adjoint imaging:
+                               swit_backward); 1 = exact discrete adjoint of the
+                               forward map (vec kernels; the forward stores the
+                               divergence term of every step, NX*LD values per
+                               step and shot, or regenerates them segment by
+                               segment with checkpoint_every: swit_backward_exact) */
 } swit_desc;
 
 /* Creates an engine and allocates its device workspace on the current device.
@@ -213,6 +220,18 @@ int swit_forward_shot_static(int32_t nx, int32_t nz, int32_t npml, int32_t nt, f
 int swit_query(const swit_engine* e, int64_t* device_bytes, int32_t* shots_per_batch, int32_t* block_x,
                int32_t* kernels_per_forward, int32_t* kernels_per_backward, int32_t* kernel_variant,
                int32_t* graph_branches);
+
+/* Exact discrete adjoint (engines created with adjoint_mode = 1) after a
+ * swit_forward with save_boundary = 1: the transpose of the forward map applied
+ * to adjoint sources adj (ns, ng_max, nt) = dJ/dseis.
+ *   grad     (nx, nz): dJ/dvp, the damping profile held fixed (it depends on vp
+ *            only through vmin, pml.f90:80); exact for perturbations that keep
+ *            vmin, e.g. <J dvp, adj> = <dvp, grad> to rounding.
+ *   src_grad (ns, nt): dJ/dsrc for the source functions given to swit_forward.
+ * Either output may be NULL; types and placement as swit_backward's.  Not a
+ * reference algorithm: fd2dmpi's own gradient is swit_backward's. */
+int swit_backward_exact(swit_engine* e, const float* adj, void* grad, void* src_grad, int32_t on_device,
+                        void* stream);
 
 /* Waits for `stream` and reports whether any kernel of the engine gave up
  * waiting for the copies it stages into shared memory (band variant: every such

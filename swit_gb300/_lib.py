@@ -15,7 +15,7 @@ ERRORS = {-1: "SWIT_E_ARG", -2: "SWIT_E_GEOM", -3: "SWIT_E_CFL", -4: "SWIT_E_MOD
 
 # every symbol include/swit_gb300.h declares
 EXPORTS = ("swit_create", "swit_set_model", "swit_forward", "swit_backward", "swit_gradient_l2",
-           "swit_export_snapshot", "swit_import_snapshot", "swit_profile_kernels", "swit_query", "swit_destroy", "swit_last_error", "swit_damp_profile",
+           "swit_export_snapshot", "swit_import_snapshot", "swit_profile_kernels", "swit_backward_exact", "swit_query", "swit_destroy", "swit_last_error", "swit_damp_profile",
            "swit_forward_shot_static", "swit_check", "swit_misfit_l2", "swit_multi_create", "swit_multi_engine",
            "swit_multi_gradient_l2", "swit_multi_misfit_l2", "swit_multi_destroy")
 
@@ -27,7 +27,7 @@ class SwitDesc(C.Structure):
                 ("rec_x", C.c_void_p), ("rec_z", C.c_void_p), ("precision", C.c_int32), ("path", C.c_int32),
                 ("shots_per_batch", C.c_int32), ("block_x", C.c_int32),
                 ("kernel_variant", C.c_int32), ("checkpoint_every", C.c_int32),
-                ("graph_branches", C.c_int32)]
+                ("graph_branches", C.c_int32), ("adjoint_mode", C.c_int32)]
 
 
 class SwitError(RuntimeError):
@@ -61,6 +61,7 @@ def load(build_if_missing: bool = True):
         "swit_export_snapshot": ([vp, vp, vp, vp, vp, i, vp], i),
         "swit_import_snapshot": ([vp, vp, vp, vp, vp, vp, i, vp], i),
         "swit_profile_kernels": ([vp, C.POINTER(C.c_int32), C.POINTER(C.c_double), vp], i),
+        "swit_backward_exact": ([vp, vp, vp, vp, C.c_int32, vp], i),
         "swit_query": ([vp, C.POINTER(C.c_int64), C.POINTER(C.c_int32), C.POINTER(C.c_int32),
                         C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.POINTER(C.c_int32)], i),
         "swit_destroy": ([vp], i),

@@ -41,23 +41,25 @@ def candidates(ns, nz_pml):
 
 
 def tune(nx, nz, npml, dx, dt, src_xz, rec_xz, vp, rho, free_surface=1, trial_steps=48, repeats=2,
-         cands=None, verbose=False):
+         cands=None, verbose=False, adjoint="fd2dmpi"):
     """Returns (best options, [(options, seconds per trial gradient), ...])."""
     import torch
     src_xz = np.asarray(src_xz, np.float32)
     rec_xz = np.asarray(rec_xz, np.float32)
     ns = src_xz.shape[0]
-    key = (nx, nz, npml, ns, rec_xz.shape[-2], trial_steps, free_surface)
+    key = (nx, nz, npml, ns, rec_xz.shape[-2], trial_steps, free_surface, adjoint)
     if key in _cache and cands is None:
         return _cache[key]
     cands = cands or candidates(ns, nz + 2 * npml)
+    if adjoint == "exact":  # the exact adjoint runs on the vec kernels
+        cands = [c for c in cands if c["kernel"] == "vec"]
     nt = trial_steps
     rng = np.random.default_rng(0)
     src = torch.from_numpy(rng.standard_normal((ns, nt)).astype(np.float32)).cuda()
     times = []
     for c in cands:
         try:
-            eng = Engine(nx, nz, npml, nt, dx, dt, src_xz, rec_xz, free_surface=free_surface, **c)
+            eng = Engine(nx, nz, npml, nt, dx, dt, src_xz, rec_xz, free_surface=free_surface, adjoint=adjoint, **c)
         except SwitError as err:  # e.g. a cluster variant whose wavefields do not fit on chip
             if verbose:
                 print("autotune", c, "unavailable:", err)

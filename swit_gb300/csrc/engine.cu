@@ -22,6 +22,7 @@
 #include "kernels_cluster.cuh"
 #include "kernels_band.cuh"
 #include "kernels_multi.cuh"
+#include "kernels_exact.cuh"
 
 using namespace swit;
 
@@ -114,6 +115,11 @@ struct swit_engine {
   cudaGraphExec_t gfwd[2] = {nullptr, nullptr};
   cudaGraphExec_t gbwd = nullptr;
   int launches_fwd = 0, launches_bwd = 0;
+  // exact discrete adjoint (adjoint_mode 1, kernels_exact.cuh): the strip buffer holds the forward's D of
+  // every step (SL = NX * LD); mirror rows, source gradient, dA/dc; graph of its reverse loop
+  int exact = 0;
+  void *xm = nullptr, *xsrc = nullptr, *xdadc = nullptr;
+  cudaGraphExec_t gxb = nullptr;
 };
 
 namespace {
@@ -145,6 +151,7 @@ void release(swit_engine* e) {
   for (int i = 0; i < 2; ++i)
     if (e->gfwd[i]) cudaGraphExecDestroy(e->gfwd[i]);
   if (e->gbwd) cudaGraphExecDestroy(e->gbwd);
+  if (e->gxb) cudaGraphExecDestroy(e->gxb);
   if (e->cap) cudaStreamDestroy(e->cap);
   for (int i = 0; i < kCapStreamsMax - 1; ++i) {
     if (e->capx[i]) cudaStreamDestroy(e->capx[i]);
@@ -154,7 +161,8 @@ void release(swit_engine* e) {
   void* ptrs[] = {e->d_zlo, e->d_zhi, e->d_ng, e->d_isx, e->d_isz, e->d_risx, e->d_risz, e->d_colptr, e->d_ig, e->d_zr, e->d_live,
                   e->d_mtrace, e->A, e->B, e->damp, e->cint, e->kp, e->ku, e->kw, e->p, e->u, e->w, e->pb, e->ub, e->wb, e->pe,
                   e->ue, e->we, e->dg, e->dfw, e->dbk, e->strips, e->src, e->seis_t, e->adj_t, e->d_in,
-                  e->d_stage, e->p2, e->u2, e->w2, e->pb2, e->ub2, e->wb2, e->pe2, e->ue2, e->we2, e->d_list, e->d_blist, e->d_bcnt, e->d_err, e->ckpt};
+                  e->d_stage, e->p2, e->u2, e->w2, e->pb2, e->ub2, e->wb2, e->pe2, e->ue2, e->we2, e->d_list, e->d_blist, e->d_bcnt, e->d_err, e->ckpt,
+                  e->xm, e->xsrc, e->xdadc};
   for (void* q : ptrs)
     if (q) cudaFree(q);
 }
@@ -361,12 +369,17 @@ void launch_forward_steps(swit_engine* e, bool store, int shot0, int nb, cudaStr
   }
   if (e->variant == 3) {
     Grid<R> g = make_grid<R>(e);
-    R* strips = store ? (R*)e->strips : nullptr;
+    // exact adjoint: the pressure phase stores D instead of the velocity phase storing strips
+    R* strips = store && !e->exact ? (R*)e->strips : nullptr;
     const dim3 block = vec_block(e), g0 = vec_grid(e, 0, nb), g1 = vec_grid(e, 1, nb);
     const VecList l0 = vec_list(e, 0), l1 = vec_list(e, 1);
     for (int it = it_lo; it <= it_hi; ++it) {
-      launch_pdl(e->pdl, k_fwd_p_v<R>, g0, block, st, g, l0, make_src(e), (const R*)e->src, (R*)e->p,
-                 (const R*)e->u, (const R*)e->w, it, shot0);
+      if (store && e->exact)
+        launch_pdl(e->pdl, k_fwd_p_vx<R>, g0, block, st, g, l0, make_src(e), (const R*)e->src, (R*)e->p,
+                   (const R*)e->u, (const R*)e->w, it, shot0, (R*)e->strips);
+      else
+        launch_pdl(e->pdl, k_fwd_p_v<R>, g0, block, st, g, l0, make_src(e), (const R*)e->src, (R*)e->p,
+                   (const R*)e->u, (const R*)e->w, it, shot0);
       launch_pdl(e->pdl, k_fwd_uw_v<R>, g1, block, st, g, l1, make_rec(e), (const R*)e->p, (R*)e->u, (R*)e->w,
                  (R*)e->seis_t, strips, it, shot0);
     }
@@ -496,6 +509,55 @@ void backward_checkpointed(swit_engine* e, int s0, int nb, cudaStream_t st) {
     e->sit0 = m * k + 1;
     launch_forward_steps<R>(e, true, s0, nb, st, std::max(2, m * k + 1), std::min(e->nt, (m + 1) * k));
     launch_backward_steps<R>(e, s0, nb, st, std::min(e->nt, (m + 1) * k + 1), m * k + 2);
+  }
+  e->sit0 = 1;
+}
+
+// Exact adjoint (kernels_exact.cuh): reverse steps it_hi .. it_lo of shots
+// [shot0, shot0+nb), two launches per step over the forward kernels' task lists.
+template <class R>
+XAdj<R> make_xadj(swit_engine* e) {
+  return XAdj<R>{(R*)e->pb, (R*)e->ub, (R*)e->wb, (R*)e->dg, (R*)e->xm, (R*)e->xsrc, (const R*)e->strips,
+                 (const R*)e->adj_t};
+}
+
+template <class R>
+void launch_exact_steps(swit_engine* e, int shot0, int nb, cudaStream_t st, int it_hi, int it_lo) {
+  Grid<R> g = make_grid<R>(e);
+  const XAdj<R> x = make_xadj<R>(e);
+  const dim3 block = vec_block(e), g0 = vec_grid(e, 0, nb), g1 = vec_grid(e, 1, nb);
+  const VecList l0 = vec_list(e, 0), l1 = vec_list(e, 1);
+  for (int it = it_hi; it >= it_lo; --it) {
+    launch_pdl(e->pdl, k_xadj_p<R>, g0, block, st, g, l0, make_rec(e), make_src(e), x, it, shot0);
+    launch_pdl(e->pdl, k_xadj_uw<R>, g1, block, st, g, l1, x, it, shot0);
+  }
+}
+
+// Exact adjoint of shots [s0, s0+nb).  Boundary saving: the forward stored D of
+// every step.  Checkpoints: per segment, last first, restore the state before
+// it, re-run its forward steps storing D into the k-step buffer, then run the
+// same steps in reverse.  Leaves sit0 = 1.
+template <class R>
+void exact_reverse(swit_engine* e, int s0, int nb, cudaStream_t st) {
+  if (!e->ckpt_k) {
+    launch_exact_steps<R>(e, s0, nb, st, e->nt, 2);
+    return;
+  }
+  const int k = e->ckpt_k;
+  const size_t fsz = (size_t)e->NX * e->LD * e->esz;
+  for (int m = e->ckpt_m - 1; m >= 0; --m) {
+    const int lo = std::max(2, m * k + 1), hi = std::min(e->nt, (m + 1) * k);
+    if (lo > hi) continue;
+    if (m > 0) {
+      ckpt_copy(e, m - 1, s0, nb, false, st);
+    } else {
+      cudaMemsetAsync((char*)e->p + (size_t)s0 * fsz, 0, (size_t)nb * fsz, st);
+      cudaMemsetAsync((char*)e->u + (size_t)s0 * fsz, 0, (size_t)nb * fsz, st);
+      cudaMemsetAsync((char*)e->w + (size_t)s0 * fsz, 0, (size_t)nb * fsz, st);
+    }
+    e->sit0 = m * k + 1;
+    launch_forward_steps<R>(e, true, s0, nb, st, lo, hi);
+    launch_exact_steps<R>(e, s0, nb, st, hi, lo);
   }
   e->sit0 = 1;
 }
@@ -682,6 +744,65 @@ int forward_impl(swit_engine* e, const float* src, void* seis, bool store, int o
   return 0;
 }
 
+// Reverse loop of the exact adjoint over all shots: plain path one shot at a
+// time, batched path captured once into a graph (batches on concurrent branches).
+template <class R>
+int run_exact_loop(swit_engine* e, cudaStream_t st) {
+  if (e->path == 1) {
+    for (int s = 0; s < e->ns; ++s) exact_reverse<R>(e, s, 1, st);
+    CK(cudaGetLastError());
+    return 0;
+  }
+  if (!e->gxb) {
+    cudaGraph_t graph;
+    CK(cudaStreamBeginCapture(e->cap, cudaStreamCaptureModeThreadLocal));
+    capture_fork(e);
+    for (int s0 = 0, b = 0; s0 < e->ns; s0 += e->batch, ++b)
+      exact_reverse<R>(e, s0, std::min(e->batch, e->ns - s0), capture_stream(e, b));
+    capture_join(e);
+    cudaError_t rc = cudaStreamEndCapture(e->cap, &graph);
+    if (rc != cudaSuccess) return fail(SWIT_E_CUDA, "exact adjoint graph capture: %s", cudaGetErrorString(rc));
+    rc = cudaGraphInstantiate(&e->gxb, graph, 0);
+    cudaGraphDestroy(graph);
+    if (rc != cudaSuccess) {
+      e->gxb = nullptr;
+      return fail(SWIT_E_CUDA, "exact adjoint graph instantiate: %s", cudaGetErrorString(rc));
+    }
+  }
+  CK(cudaGraphLaunch(e->gxb, st));
+  return 0;
+}
+
+// Exact adjoint after a storing forward run: adjoint sources already staged in
+// adj_t; grad = dJ/dvp (nx, nz), gsrc = dJ/dsrc (ns, nt), either may be null.
+template <class R>
+int exact_core(swit_engine* e, void* grad, void* gsrc, int on_device, cudaStream_t st) {
+  Grid<R> g = make_grid<R>(e);
+  const size_t fb = (size_t)e->ns * g.FSZ * e->esz;
+  CK(cudaMemsetAsync(e->pb, 0, fb, st));
+  CK(cudaMemsetAsync(e->ub, 0, fb, st));
+  CK(cudaMemsetAsync(e->wb, 0, fb, st));
+  CK(cudaMemsetAsync(e->dg, 0, fb, st));
+  CK(cudaMemsetAsync(e->xm, 0, (size_t)e->ns * 2 * e->NX * e->esz, st));
+  CK(cudaMemsetAsync(e->xsrc, 0, (size_t)e->ns * e->nt * e->esz, st));
+  int rc = run_exact_loop<R>(e, st);
+  if (rc) return rc;
+  const size_t NI = (size_t)e->nx * e->nz;
+  if (grad) {
+    void* og = on_device ? grad : e->d_stage;
+    if (e->prec == 0)
+      k_xgrad<R, float><<<nblocks(NI), 256, 0, st>>>(g, (const R*)e->dg, (const R*)e->xdadc, e->ns, (float*)og);
+    else
+      k_xgrad<R, double><<<nblocks(NI), 256, 0, st>>>(g, (const R*)e->dg, (const R*)e->xdadc, e->ns, (double*)og);
+    CK(cudaGetLastError());
+    if (!on_device) CK(cudaMemcpyAsync(grad, og, NI * e->esz, cudaMemcpyDeviceToHost, st));
+  }
+  if (gsrc)
+    CK(cudaMemcpyAsync(gsrc, e->xsrc, (size_t)e->ns * e->nt * e->esz,
+                       on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, st));
+  return 0;
+}
+
 template <class R>
 int backward_end(swit_engine* e, void* grad, void* fw, void* bk, int on_device, cudaStream_t st);
 
@@ -759,6 +880,16 @@ int backward_impl(swit_engine* e, const float* adj, void* grad, void* fw, void* 
   return backward_core<R>(e, grad, fw, bk, on_device, st);
 }
 
+template <class R>
+int exact_impl(swit_engine* e, const float* adj, void* grad, void* gsrc, int on_device, cudaStream_t st) {
+  const float* dadj;
+  int rc = stage_input(e, adj, (size_t)e->ns * e->ngmax * e->nt, on_device, st, &dadj);
+  if (rc) return rc;
+  dim3 grid((e->nt + 31) / 32, (e->ngmax + 31) / 32, e->ns), block(32, 8);
+  k_adj_in<R><<<grid, block, 0, st>>>(dadj, (R*)e->adj_t, e->ns, e->nt, e->ngmax);
+  return exact_core<R>(e, grad, gsrc, on_device, st);
+}
+
 // Waveform misfit per trace and its adjoint source syn - obs for live traces
 // (misfit.py:128-148, 263-282), from the synthetics of the last forward run.
 template <class R>
@@ -793,7 +924,7 @@ int gradient_impl(swit_engine* e, const float* src, const float* obs, void* grad
   if (rc) return rc;
   rc = residual_l2<R>(e, obs, on_device, st);
   if (rc) return rc;
-  rc = backward_core<R>(e, grad, fw, bk, on_device, st);
+  rc = e->exact ? exact_core<R>(e, grad, nullptr, on_device, st) : backward_core<R>(e, grad, fw, bk, on_device, st);
   if (rc) return rc;
   return misfit ? misfit_sum(e, st, misfit) : 0;
 }
@@ -862,6 +993,14 @@ int set_model_impl(swit_engine* e, const float* vp, const float* rho, cudaStream
   CK(cudaMemcpyAsync(e->B, B.data(), B.size() * sizeof(R), cudaMemcpyHostToDevice, st));
   CK(cudaMemcpyAsync(e->damp, damp.data(), damp.size() * sizeof(R), cudaMemcpyHostToDevice, st));
   CK(cudaMemcpyAsync(e->cint, ci.data(), ci.size() * sizeof(R), cudaMemcpyHostToDevice, st));
+  std::vector<R> dadc;
+  if (e->exact) {  // dA/dc of the exact adjoint's vp gradient
+    dadc.assign((size_t)NX * LD, R(0));
+    for (int ix = 1; ix <= NX; ++ix)
+      for (int iz = 1; iz <= NZ; ++iz)
+        dadc[(size_t)(ix - 1) * LD + (iz - 1)] = R(2.0) * at(den, iz, ix) * at(c, iz, ix) * dt / dx;
+    CK(cudaMemcpyAsync(e->xdadc, dadc.data(), dadc.size() * sizeof(R), cudaMemcpyHostToDevice, st));
+  }
   if (e->kp) {
     Grid<R> g = make_grid<R>(e);
     k_kappa<R><<<nblocks((size_t)NX * LD), 256, 0, st>>>(g, (R*)e->kp, (R*)e->ku, (R*)e->kw);
@@ -1607,6 +1746,16 @@ int swit_create(const swit_desc* d, swit_engine** out) {
     return fail(SWIT_E_ARG, "kernel_variant must be 0..6");
   }
   e->variant = d->kernel_variant ? d->kernel_variant : 3;
+  if (d->adjoint_mode < 0 || d->adjoint_mode > 1) {
+    delete e;
+    return fail(SWIT_E_ARG, "adjoint_mode must be 0 (fd2dmpi's adjoint) or 1 (exact) (got %d)", d->adjoint_mode);
+  }
+  if (d->adjoint_mode == 1 && e->variant != 3) {
+    delete e;
+    return fail(SWIT_E_ARG, "the exact adjoint runs on the vec kernels (kernel_variant 0 or 3)");
+  }
+  e->exact = d->adjoint_mode;
+  if (e->exact) e->SL = e->NX * e->LD;  // the strip buffer holds D of each step
   if (e->variant == 2 && e->LD > 1024) {
     delete e;
     return fail(SWIT_E_LIMIT, "the fused kernels need NZ + 2 npml <= 1024 (got %d)", e->NZ);
@@ -1781,6 +1930,11 @@ int swit_create(const swit_desc* d, swit_engine** out) {
   }
   AL(valloc(e, &e->strips, (size_t)ns * e->snt * e->SL));
   if (e->ckpt_k) AL(valloc(e, &e->ckpt, (size_t)e->ckpt_m * 3 * ns * FSZ));
+  if (e->exact) {
+    AL(valloc(e, &e->xm, (size_t)ns * 2 * e->NX));
+    AL(valloc(e, &e->xsrc, (size_t)ns * e->nt));
+    AL(valloc(e, &e->xdadc, FSZ));
+  }
   AL(valloc(e, &e->src, (size_t)ns * (e->nt + 1)));
   AL(valloc(e, &e->seis_t, (size_t)ns * e->nt * ngm));
   AL(valloc(e, &e->adj_t, (size_t)ns * e->nt * ngm));
@@ -1879,6 +2033,7 @@ int swit_forward(swit_engine* e, const float* src, void* seis, int save_boundary
 int swit_backward(swit_engine* e, const float* adj, void* grad, void* illum_fw, void* illum_bk, int on_device,
                   void* stream) {
   if (!e || !adj) return fail(SWIT_E_ARG, "null argument");
+  if (e->exact) return fail(SWIT_E_STATE, "the engine was created for the exact adjoint: use swit_backward_exact");
   if (!e->fwd_ready) return fail(SWIT_E_STATE, "swit_backward needs a preceding swit_forward with save_boundary=1");
   cudaStream_t st = (cudaStream_t)stream;
   int rc = e->prec ? backward_impl<double>(e, adj, grad, illum_fw, illum_bk, on_device, st)
@@ -1891,6 +2046,8 @@ int swit_backward(swit_engine* e, const float* adj, void* grad, void* illum_fw, 
 int swit_gradient_l2(swit_engine* e, const float* src, const float* obs, void* grad, void* illum_fw, void* illum_bk,
                      void* seis, double* misfit, int on_device, void* stream) {
   if (!e || !src || !obs) return fail(SWIT_E_ARG, "null argument");
+  if (e->exact && (illum_fw || illum_bk))
+    return fail(SWIT_E_ARG, "the exact adjoint computes no illumination: pass null illum_fw and illum_bk");
   if (!e->model_set) return fail(SWIT_E_STATE, "swit_set_model must be called before swit_gradient_l2");
   cudaStream_t st = (cudaStream_t)stream;
   int rc = e->prec ? gradient_impl<double>(e, src, obs, grad, illum_fw, illum_bk, seis, misfit, on_device, st)
@@ -1900,9 +2057,23 @@ int swit_gradient_l2(swit_engine* e, const float* src, const float* obs, void* g
   return 0;
 }
 
+int swit_backward_exact(swit_engine* e, const float* adj, void* grad, void* src_grad, int on_device, void* stream) {
+  if (!e || !adj) return fail(SWIT_E_ARG, "null argument");
+  if (!e->exact) return fail(SWIT_E_STATE, "the engine was created with adjoint_mode 0 (fd2dmpi's adjoint)");
+  if (!e->fwd_ready)
+    return fail(SWIT_E_STATE, "swit_backward_exact needs a preceding swit_forward with save_boundary=1");
+  cudaStream_t st = (cudaStream_t)stream;
+  int rc = e->prec ? exact_impl<double>(e, adj, grad, src_grad, on_device, st)
+                   : exact_impl<float>(e, adj, grad, src_grad, on_device, st);
+  if (rc) return rc;
+  if (!on_device) CK(cudaStreamSynchronize(st));
+  return 0;
+}
+
 int swit_export_snapshot(swit_engine* e, void* boundary, void* p_end, void* u_end, void* w_end, int on_device,
                          void* stream) {
   if (!e) return fail(SWIT_E_ARG, "null argument");
+  if (e->exact) return fail(SWIT_E_STATE, "an exact-adjoint engine keeps no boundary strips");
   if (!e->fwd_ready) return fail(SWIT_E_STATE, "no saved forward run (swit_forward with save_boundary=1)");
   cudaStream_t st = (cudaStream_t)stream;
   return e->prec ? export_impl<double>(e, boundary, p_end, u_end, w_end, on_device, st)
@@ -1913,6 +2084,7 @@ int swit_import_snapshot(swit_engine* e, const float* src, const float* boundary
                          const float* u_end, const float* w_end, int on_device, void* stream) {
   if (!e || !src || !boundary || !p_end || !u_end || !w_end) return fail(SWIT_E_ARG, "null argument");
   if (!e->model_set) return fail(SWIT_E_STATE, "swit_set_model must be called before swit_import_snapshot");
+  if (e->exact) return fail(SWIT_E_STATE, "an exact-adjoint engine keeps no boundary strips");
   cudaStream_t st = (cudaStream_t)stream;
   return e->prec ? import_impl<double>(e, src, boundary, p_end, u_end, w_end, on_device, st)
                  : import_impl<float>(e, src, boundary, p_end, u_end, w_end, on_device, st);
@@ -1920,6 +2092,7 @@ int swit_import_snapshot(swit_engine* e, const float* src, const float* boundary
 
 int swit_profile_kernels(swit_engine* e, int32_t launches[4], double mean_ms[4], void* stream) {
   if (!e || !launches || !mean_ms) return fail(SWIT_E_ARG, "null argument");
+  if (e->exact) return fail(SWIT_E_STATE, "swit_profile_kernels times fd2dmpi's adjoint (adjoint_mode 0)");
   if (!e->model_set) return fail(SWIT_E_STATE, "swit_set_model must be called first");
   cudaStream_t st = (cudaStream_t)stream;
   return e->prec ? profile_impl<double>(e, launches, mean_ms, st) : profile_impl<float>(e, launches, mean_ms, st);
@@ -1971,7 +2144,8 @@ int swit_multi_create(const swit_desc* descs, int32_t n, swit_multi** out) {
   for (int i = 0; i < n; ++i) {
     const swit_desc& d = descs[i];
     if (d.nx + 2 * d.npml > 16384 || d.ns > 65535) return fail(SWIT_E_LIMIT, "instance %d: more than 16384 PML-grid columns", i);
-    if (d.precision != 0 || d.path != 0 || (d.kernel_variant != 0 && d.kernel_variant != 3) || d.checkpoint_every)
+    if (d.precision != 0 || d.path != 0 || (d.kernel_variant != 0 && d.kernel_variant != 3) || d.checkpoint_every ||
+        d.adjoint_mode)
       return fail(SWIT_E_ARG,
                   "instance %d: a multi-instance engine runs FP32 vec kernels on the batched path with boundary saving",
                   i);

@@ -166,14 +166,21 @@ __device__ __forceinline__ void col_window(const R* f, const VecIdx& v, int LD4,
 }
 
 // ---------------------------------------------------------------------------
-// Forward pressure phase (fdcore.f90:77-94).
-template <class R, int T>
+// Forward pressure phase (fdcore.f90:77-94).  SAVE: also store the divergence
+// term D of every updated row into dsave (the step's record; 0 elsewhere), for
+// the exact adjoint (kernels_exact.cuh).
+template <class R, int T, bool SAVE = false>
 __device__ __forceinline__ void fwd_p_body(const Grid<R>& g, const Sources& src, const R* __restrict__ s_fwd, R* __restrict__ p,
                                            const R* __restrict__ u, const R* __restrict__ w, int it,
-                                           const VecIdx& v) {
+                                           const VecIdx& v, R* __restrict__ dsave = nullptr) {
   constexpr bool CHK = T == 2;
   const int LD4 = g.LD >> 2, ix = v.ix, iz0 = v.iz0, fs = g.fs, NZ = g.NZ;
   V4<R> pv = ld4(p, v.k4);
+  V4<R> dv;
+  if constexpr (SAVE) {
+#pragma unroll
+    for (int j = 0; j < 4; ++j) dv.x[j] = R(0);
+  }
   bool dirty = false;
   if (!CHK || (ix >= 3 && ix <= g.NX - 2 && iz0 + 3 >= fs + 1 && iz0 <= NZ - 2)) {
     const V4<R> a = ld4(g.A, v.kc);
@@ -186,9 +193,10 @@ __device__ __forceinline__ void fwd_p_body(const Grid<R>& g, const Sources& src,
       const int iz = iz0 + j;
       if (!CHK || (iz >= fs + 1 && iz <= NZ - 2)) {
         const R kappa = T == 0 ? R(0) : kk.x[j];
-        pv.x[j] = (R(1.0) - kappa) * pv.x[j] -
-                  a.x[j] * (g.c1 * (u0.x[j] - um1.x[j] + wz[j + 2] - wz[j + 1]) +
-                            g.c2 * (up1.x[j] - um2.x[j] + wz[j + 3] - wz[j]));
+        const R D = g.c1 * (u0.x[j] - um1.x[j] + wz[j + 2] - wz[j + 1]) +
+                    g.c2 * (up1.x[j] - um2.x[j] + wz[j + 3] - wz[j]);
+        pv.x[j] = (R(1.0) - kappa) * pv.x[j] - a.x[j] * D;
+        if constexpr (SAVE) dv.x[j] = D;
       }
     }
     dirty = true;
@@ -213,6 +221,7 @@ __device__ __forceinline__ void fwd_p_body(const Grid<R>& g, const Sources& src,
     }
   }
   if (dirty) st4(p, v.k4, pv);
+  if constexpr (SAVE) st4(dsave, v.k4, dv);
 }
 
 // Body tier of a vector in each phase: 0 = fast (deep interior: no damping, no

@@ -28,7 +28,7 @@ class Engine:
 
     def __init__(self, nx, nz, npml, nt, dx, dt, src_xz, rec_xz, free_surface=1, ng=None, precision="fp32",
                  path="batched", shots_per_batch=0, block_x=0, kernel="auto", checkpoint_every=0, graph_branches=0,
-                 _borrow=None):
+                 adjoint="fd2dmpi", _borrow=None):
         lib = _lib.load()
         src_xz = np.asarray(src_xz, dtype=np.float32).reshape(-1, 2)
         rec_xz = np.asarray(rec_xz, dtype=np.float32)
@@ -47,6 +47,9 @@ class Engine:
             raise ValueError("path must be 'batched' or 'plain'")
         self.path = path
         variants = {"auto": 0, "split": 1, "fused": 2, "vec": 3, "cluster": 4, "hybrid": 5, "band": 6}
+        if adjoint not in ("fd2dmpi", "exact"):
+            raise ValueError("adjoint must be 'fd2dmpi' or 'exact'")
+        self.adjoint = adjoint
         if kernel not in variants:
             raise ValueError("kernel must be one of %s" % ", ".join(sorted(variants)))
         self._keep = dict(
@@ -58,7 +61,7 @@ class Engine:
                           self.ngmax, k["ng"].ctypes.data, k["xs"].ctypes.data, k["zs"].ctypes.data,
                           k["xg"].ctypes.data, k["zg"].ctypes.data, 1 if self.fp64 else 0,
                           1 if path == "plain" else 0, int(shots_per_batch), int(block_x), variants[kernel],
-                          int(checkpoint_every), int(graph_branches))
+                          int(checkpoint_every), int(graph_branches), 1 if adjoint == "exact" else 0)
         self.checkpoint_every = int(checkpoint_every)
         self._desc = d
         self._lib = lib
@@ -146,14 +149,30 @@ class Engine:
         _lib.check(self._lib.swit_backward(self._h, pa, ptrs[0], ptrs[1], ptrs[2], dev, self._stream(dev)))
         return tuple(outs)
 
+    def backward_exact(self, adj, grad=None, src_grad=None):
+        """Exact discrete adjoint (engines with adjoint="exact") of adjoint sources
+        adj (ns, ng_max, nt) = dJ/dseis after forward(save_boundary=True): returns
+        (grad (nx, nz) = dJ/dvp with the damping profile held fixed,
+        src_grad (ns, nt) = dJ/dsrc)."""
+        adj = self._f32(adj)
+        if tuple(adj.shape) != (self.ns, self.ngmax, self.nt):
+            raise ValueError("adj must be (ns, ng_max, nt)")
+        pa, dev = self._ptr(adj, np.float32)
+        grad = grad if grad is not None else self._new((self.nx, self.nz), dev)
+        src_grad = src_grad if src_grad is not None else self._new((self.ns, self.nt), dev)
+        _lib.check(self._lib.swit_backward_exact(self._h, pa, self._ptr(grad, self.out_dtype)[0],
+                                                 self._ptr(src_grad, self.out_dtype)[0], dev, self._stream(dev)))
+        return grad, src_grad
+
     def gradient_l2(self, src, obs, return_seis=False):
-        """Waveform-misfit gradient: returns dict(grad, illum_fw, illum_bk, misfit[, seis])."""
+        """Waveform-misfit gradient: returns dict(grad, illum_fw, illum_bk, misfit[, seis])
+        (exact-adjoint engines: the exact gradient and no illumination)."""
         src, obs = self._f32(src), self._f32(obs)
         ps, dev = self._ptr(src, np.float32)
         po, dev2 = self._ptr(obs, np.float32)
         if dev != dev2:
             raise ValueError("src and obs must both be host or both be device arrays")
-        outs = [self._new((self.nx, self.nz), dev) for _ in range(3)]
+        outs = [self._new((self.nx, self.nz), dev) if k == 0 or self.adjoint == "fd2dmpi" else None for k in range(3)]
         seis = self._new((self.ns, self.ngmax, self.nt), dev) if return_seis else None
         m = C.c_double(0.0)
         _lib.check(self._lib.swit_gradient_l2(self._h, ps, po, *[self._ptr(x, self.out_dtype)[0] for x in outs],
