@@ -13,8 +13,15 @@ continuous-adjoint imaging gradient of fd2dmpi, not the exact transpose of the
 discrete forward map (the central finite-difference agreement is measured by
 tests/test_gpu_autograd.py).
 
+With an engine created with adjoint="exact" the backward is the exact
+transpose of the discrete forward map instead (swit_backward_exact): vp.grad
+is dL/dvp with the damping profile held fixed (it follows vp only through
+vmin), and src.grad is dL/dsrc; torch.autograd.gradcheck holds with the FP64
+build (tests/test_gpu_exact.py).
+
 If the engine ran another forward between this forward and its backward, the
-boundary strips are recomputed first (checkpointed recomputation).
+boundary strips (or, for the exact adjoint, the stored divergence terms) are
+recomputed first.
 """
 import torch
 
@@ -38,11 +45,16 @@ class _Propagate(torch.autograd.Function):
             engine.set_model(vp.detach().contiguous().float(), rho.detach().contiguous().float())
             engine.forward(src.detach().contiguous().float(), save_boundary=True)
             engine._generation += 1
-        g, _, _ = engine.backward(grad_seis.detach().contiguous().float())
+        adj = grad_seis.detach().contiguous().float()
+        if getattr(engine, "adjoint", "fd2dmpi") == "exact":
+            g, gs = engine.backward_exact(adj)
+            return g.to(vp.dtype), None, (gs.to(src.dtype) if ctx.needs_input_grad[2] else None), None
+        g, _, _ = engine.backward(adj)
         g = g / engine.dt
         return g.to(vp.dtype), None, None, None
 
 
 def propagate(engine, vp, rho, src):
-    """Differentiable forward modeling of every shot (gradient w.r.t. vp only)."""
+    """Differentiable forward modeling of every shot: gradients w.r.t. vp, and
+    w.r.t. src for exact-adjoint engines."""
     return _Propagate.apply(vp, rho, src, engine)

@@ -149,3 +149,50 @@ def test_exact_and_fd2dmpi_calls_refuse_the_other_mode(base):
         e.forward(base["src"], save_boundary=True)
         with pytest.raises(SwitError, match="SWIT_E_STATE"):
             e.backward_exact(base["adj"])
+
+
+def test_autograd_uses_the_exact_adjoint(base):
+    import torch
+    from swit_gb300.autograd import propagate
+    s = base["s"]
+    rho = torch.from_numpy(base["rho"]).cuda()
+    with engine(s) as e:
+        vp = torch.from_numpy(s.vp_true).cuda().requires_grad_(True)
+        src = torch.from_numpy(base["src"]).cuda().requires_grad_(True)
+        r = torch.from_numpy(base["adj"]).cuda()
+        (propagate(e, vp, rho, src) * r).sum().backward()
+    np.testing.assert_array_equal(vp.grad.cpu().numpy(), base["ref"]["g"])
+    np.testing.assert_array_equal(src.grad.cpu().numpy(), base["ref"]["gsrc"])
+
+
+def test_gradcheck_with_the_fp64_exact_adjoint():
+    """torch.autograd.gradcheck of seismogram samples with respect to vp at a few
+    points (perturbations of 0.5 m/s: exact in the FP32 model input, away from
+    vmin) and to the source samples."""
+    import torch
+    from swit_gb300.autograd import propagate
+    s = survey.small(nx=24, nz=16, npml=6, nt=160, ns=2)
+    rho = torch.from_numpy(s.rho(s.vp_true)).cuda()
+    vp0 = torch.from_numpy(s.vp_true).cuda().double()
+    vmin = float(vp0[:, 1:].min())
+    rng = np.random.default_rng(8)
+    cand = [(i, j) for i in range(2, s.nx - 2) for j in range(1, s.nz - 1) if s.vp_true[i, j] > vmin + 50]
+    pts = [cand[k] for k in rng.choice(len(cand), 10, replace=False)]
+    ii = torch.tensor([p[0] for p in pts], device="cuda")
+    jj = torch.tensor([p[1] for p in pts], device="cuda")
+    src0 = torch.from_numpy(s.source()).cuda().double()
+    with Engine(**s.engine_args(), precision="fp64", adjoint="exact") as e:
+        scale = float(propagate(e, vp0, rho, src0)[:, ::4, ::16].abs().max())  # outputs of order 1
+
+        def f_vp(x):
+            vp = vp0.index_put((ii, jj), vp0[ii, jj] + x)
+            return propagate(e, vp, rho, src0)[:, ::4, ::16] / scale
+
+        x = torch.zeros(len(pts), dtype=torch.float64, device="cuda", requires_grad=True)
+        assert torch.autograd.gradcheck(f_vp, (x,), eps=0.5, atol=1e-7, rtol=1e-4, fast_mode=False)
+
+        def f_src(sv):
+            return propagate(e, vp0, rho, sv)[:, ::4, ::16] / scale
+
+        sv = src0.clone().requires_grad_(True)
+        assert torch.autograd.gradcheck(f_src, (sv,), eps=2.0 ** -6, atol=1e-7, rtol=1e-4, fast_mode=True)
