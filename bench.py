@@ -49,9 +49,11 @@ def parse():
     ap.add_argument("--kernel", default="auto", choices=["auto", "fused", "split", "vec", "cluster", "hybrid", "band"])
     ap.add_argument("--no-tune", action="store_true", help="skip the launch-configuration autotuner")
     ap.add_argument("--no-extras", action="store_true", help="skip plain path, CPU baseline and kernel profile")
-    ap.add_argument("--workload", default="marmousi", choices=["marmousi", "large", "multi"],
+    ap.add_argument("--workload", default="marmousi", choices=["marmousi", "large", "multi", "correlation"],
                     help="marmousi: 481x141 nt 4000 49 shots (the headline); large: 2001x601 nt 6000 200 shots; "
-                         "multi: uneven independent FWI problems, L-BFGS on all at once vs one after another")
+                         "multi: uneven independent FWI problems, L-BFGS on all at once vs one after another; "
+                         "correlation: 501x171 nt 5000 51 shots, global-correlation + traveltime misfits "
+                         "through torch.autograd")
     ap.add_argument("--instances", type=int, default=64, help="multi: problems")
     ap.add_argument("--iters", type=int, default=5, help="multi: L-BFGS iterations")
     ap.add_argument("--scale", type=float, default=1.0, help="multi: factor on shot counts and record lengths")
@@ -519,12 +521,93 @@ def run_multi(args):
     print(json.dumps(line), flush=True)
 
 
+def run_correlation(args):
+    """The differentiable path with correlation misfits at 501x171, nt 5000, 51
+    shots: seismograms from autograd.propagate, normalised global-correlation
+    plus cross-correlation traveltime misfit (swit_gb300.misfit, the reference's
+    adjoint sources), loss.backward() through the engine's reverse loop (fd2dmpi's
+    adjoint, or the exact adjoint with --adjoint exact).  A step is one such
+    gradient of every shot."""
+    import torch
+
+    from swit_gb300 import Engine, misfit, survey
+    from swit_gb300.autograd import propagate
+    sv = survey.config(2, ns=args.shots, nt=args.nt)
+    ckpt = int(args.checkpoint) if args.checkpoint != "auto" else 0
+    opts = dict(shots_per_batch=args.batch, block_x=args.block_x, graph_branches=args.branches, adjoint=args.adjoint,
+                checkpoint_every=ckpt)
+    eng = Engine(**sv.engine_args(), kernel="vec" if args.kernel == "auto" else args.kernel, **opts)
+    q = eng.query()
+    rho = torch.from_numpy(sv.rho(sv.vp_true)).cuda()
+    src = torch.from_numpy(sv.source()).cuda()
+    eng.set_model(torch.from_numpy(sv.vp_true).cuda(), rho)
+    obs = eng.forward(src, save_boundary=False).clone()
+    vp0 = torch.from_numpy(sv.vp_init).cuda()
+
+    def step(vp_in, src_in, obs_in):
+        vp = vp_in.clone().requires_grad_(True)
+        seis = propagate(eng, vp, rho, src_in)
+        loss = misfit.global_correlation(seis, obs_in, sv.dt) + misfit.traveltime(seis, obs_in, sv.dt)
+        loss.backward()
+        return vp.grad, loss.detach()
+
+    for _ in range(args.warmup):
+        step(vp0, src, obs)
+    torch.cuda.synchronize()
+    clocks = ClockSampler(0)
+    clocks.start()
+    time.sleep(0.3)
+    stream = torch.cuda.current_stream()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    for _ in range(args.steps):
+        g, loss = step(vp0, src, obs)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    ms_per_step = ev0.elapsed_time(ev1) / args.steps
+    value = sv.ns / (ms_per_step / 1000.0)
+    # end to end: model, sources and observed data from pinned host memory, gradient and misfit back
+    vp_h, src_h, obs_h = vp0.cpu().pin_memory(), src.cpu().pin_memory(), obs.cpu().pin_memory()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        gg, ll = step(vp_h.cuda(non_blocking=True), src_h.cuda(non_blocking=True), obs_h.cuda(non_blocking=True))
+        gg.cpu(), ll.cpu()
+    torch.cuda.synchronize()
+    e2e_s = (time.perf_counter() - t0) / args.steps
+    U, B = work_units(sv.nx, sv.nz, sv.npml, sv.nt, sv.ng)
+    peak, peak_kind = measured_peak()
+    gh = g.double().cpu().numpy()
+    line = {"metric": "FWI shot-gradients/s (501x171, nt=5000) global-correlation + traveltime misfits through "
+                      "torch.autograd", "value": value, "unit": "shot-gradients/s", "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": sv.name, "grid": [sv.nx, sv.nz], "npml": sv.npml, "nt": sv.nt, "shots": sv.ns,
+                       "receivers": sv.ng, "dx_m": sv.dx, "dt_s": sv.dt, "adjoint": args.adjoint,
+                       "kernel": q["kernel"], "shots_per_launch": q["shots_per_batch"],
+                       "graph_branches": q["graph_branches"],
+                       "memory": {"strategy": "checkpoints every %d steps" % ckpt if ckpt else "stored per step",
+                                  "device_bytes": q["device_bytes"]},
+                       "l2": "inputs larger than L2: each step streams the per-step records of every shot",
+                       "gradient_l2": float(np.linalg.norm(gh)), "loss": float(loss)},
+            "gpts_per_s": value * U / 1e9, "hbm_roof_frac_step": value * B / 1e9 / peak, "peak_kind": peak_kind,
+            "e2e": {"value": sv.ns / e2e_s, "unit": "shot-gradients/s",
+                    "h2d_bytes_per_step": int(vp_h.numel() * 4 + src_h.numel() * 4 + obs_h.numel() * 4),
+                    "d2h_bytes_per_step": int(sv.nx * sv.nz * 4 + 4)},
+            "clocks": clk,
+            "gpu_launches": int(args.steps * (q["kernels_per_forward"] + q["kernels_per_backward"] + 5))}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         run_reference(args)
     elif args.workload == "multi":
         run_multi(args)
+    elif args.workload == "correlation":
+        run_correlation(args)
     else:
         run_mine(args)
 

@@ -131,6 +131,32 @@ def faulted_layers(nx=481, nz=141, dx=25.0, seed=1001, nlayers=30, vmin=1500.0, 
     return np.clip(vp, vmin, vmax * (1 + noise)).astype(np.float32)
 
 
+def thrust_fold(nx=501, nz=171, dx=20.0, seed=1002, nlayers=25, vmin=2000.0, vmax=6000.0, amp=(300.0, 800.0),
+                nthrust=2, offset=(200.0, 500.0)):
+    """Thrust-fold model: nlayers layers vmin..vmax (increasing with depth) folded by
+    one Gaussian anticline of amplitude amp and cut by nthrust thrust faults (dip
+    25-40 degrees) whose hanging walls are raised by offset."""
+    rng = np.random.default_rng(seed)
+    x = np.arange(nx) * dx
+    z = np.arange(nz) * dx
+    X, Z = np.meshgrid(x, z, indexing="ij")
+    a = rng.uniform(*amp)
+    xc = rng.uniform(0.3, 0.7) * x[-1]
+    width = rng.uniform(0.15, 0.3) * x[-1]
+    zeff = Z + a * np.exp(-((X - xc) / width) ** 2)  # layers pushed up over the anticline
+    for _ in range(nthrust):
+        xf = rng.uniform(0.2, 0.8) * x[-1]
+        ang = rng.uniform(25.0, 40.0) * np.pi / 180.0
+        side = rng.choice([-1.0, 1.0])
+        hanging = Z < side * (X - xf) * np.tan(ang)  # above the fault plane
+        zeff = np.where(hanging, zeff + rng.uniform(*offset), zeff)
+    depths = np.linspace(zeff.min(), zeff.max(), nlayers + 1)[1:-1]  # every layer appears in the section
+    depths = depths + rng.uniform(-0.2, 0.2, depths.shape) * (depths[1] - depths[0])
+    idx = np.searchsorted(np.sort(depths), zeff)
+    vel = np.linspace(vmin, vmax, nlayers)
+    return vel[np.clip(idx, 0, nlayers - 1)].astype(np.float32)
+
+
 def smooth_layered_random(nx=2001, nz=601, dx=10.0, seed=1003, vmin=1500.0, vmax=5000.0, nlayers=12,
                           corr_m=200.0, std=0.04):
     """Smooth-plus-layered model vmin..vmax with a 2-D Gaussian-correlated random field (relative std, correlation
@@ -157,7 +183,7 @@ def smooth(vp, sigma_m, dx, keep_top=0):
 
 def config(idx, ns=None, nt=None):
     """The seeded survey of benchmark configuration idx (0: plain small, 1: batched Marmousi-like,
-    3: large memory-bound case)."""
+    2: correlation misfits on a thrust-fold model, 3: large memory-bound case)."""
     if idx == 0:
         nx, nz, dx, dt, nt_, npml, f0 = 201, 101, 25.0, 0.002, 2000, 40, 5.0
         vp = layered_anomaly(nx, nz, dx, seed=1000)
@@ -170,6 +196,12 @@ def config(idx, ns=None, nt=None):
         init = smooth(vp, 250.0, dx, keep_top=12)
         src, rec = _line_geometry(nx, dx, 49 if ns is None else ns, 25.0, 25.0)
         name = "marmousi-like 481x141 dx25 nt4000 49 shots"
+    elif idx == 2:
+        nx, nz, dx, dt, nt_, npml, f0 = 501, 171, 20.0, 0.0015, 5000, 40, 5.0
+        vp = thrust_fold(nx, nz, dx, seed=1002)
+        init = smooth(vp, 250.0, dx)
+        src, rec = _line_geometry(nx, dx, 51 if ns is None else ns, 20.0, 20.0)
+        name = "thrust-fold 501x171 dx20 nt5000 51 shots"
     elif idx == 3:
         nx, nz, dx, dt, nt_, npml, f0 = 2001, 601, 10.0, 0.001, 6000, 60, 10.0
         vp = smooth_layered_random(nx, nz, dx, seed=1003)

@@ -6,7 +6,8 @@ import pytest
 from swit_gb300 import survey
 
 
-@pytest.mark.parametrize("idx,shape,ns,ng,nt", [(0, (201, 101), 5, 201, 2000), (1, (481, 141), 49, 481, 4000)])
+@pytest.mark.parametrize("idx,shape,ns,ng,nt", [(0, (201, 101), 5, 201, 2000), (1, (481, 141), 49, 481, 4000),
+                                                (2, (501, 171), 51, 501, 5000)])
 def test_config_shapes_and_stability(idx, shape, ns, ng, nt):
     s = survey.config(idx)
     assert s.vp_true.shape == shape and s.vp_init.shape == shape
@@ -29,3 +30,17 @@ def test_source_is_the_integrated_reference_ricker():
     assert abs(np.argmax(w) * 0.002 - 1.2 / 5.0) < 0.002
     s = survey.integrated_source(w)
     np.testing.assert_allclose(s[1:], np.cumsum(0.5 * (w[1:] + w[:-1])).astype(np.float32), rtol=1e-5, atol=1e-7)
+
+
+def test_thrust_fold_model():
+    """501x171 at 20 m: 25 layers from 2000 to 6000 m/s, increasing with depth on
+    average, folded (layer boundaries not flat) and seeded."""
+    s = survey.config(2)
+    vp = s.vp_true
+    assert np.unique(vp).size == 25 and vp.min() == 2000.0 and vp.max() == 6000.0
+    mean_z = vp.mean(axis=0)
+    assert mean_z[-1] > mean_z[0] + 2500
+    top_layer_depth = (vp <= vp.min()).sum(axis=1)
+    assert top_layer_depth.max() - top_layer_depth.min() >= 5  # the anticline bends the layers
+    np.testing.assert_array_equal(vp, survey.config(2).vp_true)
+    assert s.dt == 0.0015 and s.dx == 20.0
