@@ -80,11 +80,15 @@ __device__ __forceinline__ void vec_flags(const Grid<R>& g, VecIdx& v) {
   v.deep = v.ix >= g.L + 3 && v.ix <= g.NX - g.L - 3 && v.iz0 >= g.L + 4 && v.iz0 + 3 <= g.NZ - g.L - 3;
 }
 
-// Resident 256-thread blocks per SM the vec step kernels are compiled for
-// (caps their registers at 65536 / (256 * SWIT_VEC_MINB)).
+// Resident 256-thread blocks per SM the FP32 vec step kernels are compiled for
+// (caps their registers at 65536 / (256 * SWIT_VEC_MINB)); the FP64 builds are
+// not capped.  4 (64 registers, no spill) measured 2-5 % faster than the
+// uncapped build (70-72 registers in k_bwd_p_v and k_fwd_uw_v, 3 blocks per SM);
+// 5 and 6 spill and are slower.
 #ifndef SWIT_VEC_MINB
-#define SWIT_VEC_MINB 1
+#define SWIT_VEC_MINB 4
 #endif
+#define SWIT_VEC_MINB_R(R) (sizeof(R) == 4 ? SWIT_VEC_MINB : 1)
 
 // Programmatic dependent launch: wait until the previous kernel in the stream
 // has completed and its writes are visible, then let the next kernel's blocks
@@ -295,7 +299,7 @@ __device__ __forceinline__ int tier_bwd_p(const Grid<R>& g, const VecIdx& v, boo
   } while (0)
 
 template <class R>
-__global__ void __launch_bounds__(256, SWIT_VEC_MINB) k_fwd_p_v(Grid<R> g, VecList L, Sources src, const R* __restrict__ s_fwd, R* P,
+__global__ void __launch_bounds__(256, SWIT_VEC_MINB_R(R)) k_fwd_p_v(Grid<R> g, VecList L, Sources src, const R* __restrict__ s_fwd, R* P,
                                                  const R* __restrict__ U, const R* __restrict__ W, int it, int shot0) {
   VecIdx v;
   int t;
@@ -414,7 +418,7 @@ __device__ __forceinline__ void fwd_uw_body(const Grid<R>& g, const Receivers& r
 }
 
 template <class R>
-__global__ void __launch_bounds__(256, SWIT_VEC_MINB) k_fwd_uw_v(Grid<R> g, VecList L, Receivers rec, const R* __restrict__ P, R* U,
+__global__ void __launch_bounds__(256, SWIT_VEC_MINB_R(R)) k_fwd_uw_v(Grid<R> g, VecList L, Receivers rec, const R* __restrict__ P, R* U,
                                                   R* W, R* __restrict__ seis_t, R* __restrict__ strips, int it,
                                                   int shot0) {
   VecIdx v;
@@ -528,7 +532,7 @@ __device__ __forceinline__ void bwd_uw_body(const Grid<R>& g, const R* __restric
 }
 
 template <class R>
-__global__ void __launch_bounds__(256, SWIT_VEC_MINB) k_bwd_uw_v(Grid<R> g, VecList L, const R* __restrict__ PB, R* UB, R* WB,
+__global__ void __launch_bounds__(256, SWIT_VEC_MINB_R(R)) k_bwd_uw_v(Grid<R> g, VecList L, const R* __restrict__ PB, R* UB, R* WB,
                                                   const R* __restrict__ PE, R* UE, R* WE,
                                                   const R* __restrict__ strips, int it, int shot0) {
   VecIdx v;
@@ -658,7 +662,7 @@ __device__ __forceinline__ void bwd_p_body(const Grid<R>& g, const Receivers& re
 
 // dg, dfw, dbk are the shot's imaging sums (indexed by v.kg).
 template <class R>
-__global__ void __launch_bounds__(256, SWIT_VEC_MINB) k_bwd_p_v(Grid<R> g, VecList L, Receivers rec, Sources src,
+__global__ void __launch_bounds__(256, SWIT_VEC_MINB_R(R)) k_bwd_p_v(Grid<R> g, VecList L, Receivers rec, Sources src,
                                                  const R* __restrict__ s_fwd, const R* __restrict__ adj_t, R* PB,
                                                  const R* __restrict__ UB, const R* __restrict__ WB, R* PE,
                                                  const R* __restrict__ UE, const R* __restrict__ WE, R* DG, R* DFW,
