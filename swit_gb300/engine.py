@@ -110,8 +110,12 @@ class Engine:
 
     @staticmethod
     def _f32(a):
+        """float32, C-contiguous; host inputs that already are keep their buffer (a
+        pinned torch tensor stays pinned, so the engine's copy is a direct DMA)."""
         if _is_torch(a):
-            return a.contiguous().float() if a.is_cuda else a.detach().cpu().numpy().astype(np.float32)
+            if a.is_cuda:
+                return a.contiguous().float()
+            return np.ascontiguousarray(a.detach().numpy(), dtype=np.float32)
         return np.ascontiguousarray(a, dtype=np.float32)
 
     # ------------------------------------------------------------------ API
