@@ -192,6 +192,51 @@ def cpu_baseline(sv, rho, src, obs, threads, kind="port"):
             "sample": "%d of %d shots at full nt=%d, one shot per thread, %.1f s wall" % (n, sv.ns, sv.nt, wall)}
 
 
+def cpu_with_strip_io(sv, rho, src, obs, threads):
+    """The same sample as cpu_baseline, but with fd2dmpi's file round trip: the
+    forward job writes each shot's boundary strips and final wavefields to files
+    (fdcore.f90:130-166, one file set per shot, srcN_snapshot/), the adjoint job
+    reads them back (solver.f90:213-228).  Files go to a temporary directory,
+    written and read by one thread per shot."""
+    import shutil
+    import tempfile
+    from concurrent.futures import ThreadPoolExecutor
+
+    from oracle import oracle as O
+    n = min(sv.ns, threads)
+    pb = O.Problem(sv.nx, sv.nz, sv.npml, sv.nt, sv.dx, sv.dt, sv.src_xz[:n], sv.rec_xz[:n])
+    keys = ("boundary", "p_end", "u_end", "w_end")
+    tmp = tempfile.mkdtemp(prefix="swit_strips_")
+    try:
+        t0 = time.perf_counter()
+        f = O.forward(pb, sv.vp_init, rho, src[:n], store=True, nthreads=threads)
+        shapes = {k: f[k].shape[1:] for k in keys}
+
+        def write(i):
+            for k in keys:
+                f[k][i].tofile(os.path.join(tmp, "src%d_%s.bin" % (i + 1, k)))
+
+        def read(i):
+            return [np.fromfile(os.path.join(tmp, "src%d_%s.bin" % (i + 1, k)), np.float32).reshape(shapes[k])
+                    for k in keys]
+
+        with ThreadPoolExecutor(threads) as ex:
+            list(ex.map(write, range(n)))
+            for k in keys:
+                del f[k]
+            parts = list(ex.map(read, range(n)))
+        fwd = {k: np.stack([p[j] for p in parts]) for j, k in enumerate(keys)}
+        adj = (f["seis"] - obs[:n]).astype(np.float32)
+        O.adjoint(pb, sv.vp_init, rho, src[:n], adj, fwd, nthreads=threads)
+        wall = time.perf_counter() - t0
+        nbytes = sum(os.path.getsize(os.path.join(tmp, x)) for x in os.listdir(tmp))
+    finally:
+        shutil.rmtree(tmp, ignore_errors=True)
+    return {"value": n / wall, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": "%d of %d shots at full nt=%d with the strips and final wavefields written to and read from "
+                      "files (%.2f GB), %.1f s wall" % (n, sv.ns, sv.nt, nbytes / 1e9, wall)}
+
+
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -222,6 +267,8 @@ def run_reference(args):
                              "sample": "%d of %d shots per step at full nt, one shot per thread" % (n, sv.ns)},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
             "gpts_per_s": v * U / 1e9}
+    # fd2dmpi keeps the strips on disk between its forward and adjoint jobs: one timing with that round trip
+    line["cpu_baseline_with_strip_io"] = cpu_with_strip_io(sv, rho, src, obs, threads)
     print(json.dumps(line), flush=True)
 
 
