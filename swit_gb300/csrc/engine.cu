@@ -10,6 +10,7 @@
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <utility>
@@ -112,14 +113,16 @@ struct swit_engine {
   cudaStream_t capx[kCapStreamsMax - 1] = {};
   cudaEvent_t ev_fork = nullptr, ev_join[kCapStreamsMax - 1] = {};
   int branches = 2;  // graph branches in use (swit_desc.graph_branches)
-  cudaGraphExec_t gfwd[2] = {nullptr, nullptr};
-  cudaGraphExec_t gbwd = nullptr;
+  // captured loops, each a sequence of graphs of at most kGraphNodes nodes (capture_chunked)
+  std::vector<cudaGraphExec_t> gfwd[2];
+  std::vector<cudaGraphExec_t> gbwd;
   int launches_fwd = 0, launches_bwd = 0;
   // exact discrete adjoint (adjoint_mode 1, kernels_exact.cuh): the strip buffer holds the forward's D of
   // every step (SL = NX * LD); mirror rows, source gradient, dA/dc; graph of its reverse loop
   int exact = 0;
   void *xm = nullptr, *xsrc = nullptr, *xdadc = nullptr;
-  cudaGraphExec_t gxb = nullptr;
+  std::vector<cudaGraphExec_t> gxb;
+  size_t graph_nodes = 0;  // node bound per captured graph (kGraphNodes; SWIT_GRAPH_NODES overrides)
 };
 
 namespace {
@@ -148,10 +151,10 @@ int valloc(swit_engine* e, void** ptr, size_t n) {
 }
 
 void release(swit_engine* e) {
-  for (int i = 0; i < 2; ++i)
-    if (e->gfwd[i]) cudaGraphExecDestroy(e->gfwd[i]);
-  if (e->gbwd) cudaGraphExecDestroy(e->gbwd);
-  if (e->gxb) cudaGraphExecDestroy(e->gxb);
+  for (auto* v : {&e->gfwd[0], &e->gfwd[1], &e->gbwd, &e->gxb}) {
+    for (cudaGraphExec_t x : *v) cudaGraphExecDestroy(x);
+    v->clear();
+  }
   if (e->cap) cudaStreamDestroy(e->cap);
   for (int i = 0; i < kCapStreamsMax - 1; ++i) {
     if (e->capx[i]) cudaStreamDestroy(e->capx[i]);
@@ -586,6 +589,64 @@ inline void capture_join(swit_engine* e) {
   }
 }
 
+// A captured loop is split into graphs of at most about kGraphNodes nodes,
+// each a whole number of rounds of the branches.  Observed on GB300: a 200-shot,
+// nt 6000 survey in one-shot batches captured as one graph of 2.4 M kernel
+// nodes per loop returned a NaN gradient, and capturing a 4.8 M-node loop
+// crashed the process, where graphs of up to 0.5 M nodes ran correctly.
+constexpr size_t kGraphNodes = size_t(1) << 18;
+
+// Upper bound of the nodes one batch adds to a captured loop.
+inline size_t loop_nodes(const swit_engine* e) {
+  return 2 * (size_t)(e->nt - 1) * (e->ckpt_k ? 2 : 1) + 8 * (size_t)e->ckpt_m + 8;
+}
+
+inline void destroy_graphs(std::vector<cudaGraphExec_t>& ex) {
+  for (cudaGraphExec_t x : ex) cudaGraphExecDestroy(x);
+  ex.clear();
+}
+
+inline int launch_graphs(const std::vector<cudaGraphExec_t>& ex, cudaStream_t st) {
+  for (cudaGraphExec_t x : ex) CK(cudaGraphLaunch(x, st));
+  return 0;
+}
+
+// Captures batches 0 .. nbatch-1 (issue(b, stream) launches batch b's work on
+// the given capture stream) into ex: consecutive chunks of batches, each chunk
+// one graph with the batches on concurrent branches.  ex is left empty on error.
+template <class F>
+int capture_chunked(swit_engine* e, std::vector<cudaGraphExec_t>& ex, int nbatch, size_t nodes_per_batch,
+                    const char* what, F&& issue) {
+  int chunk = (int)std::max<size_t>(1, e->graph_nodes / std::max<size_t>(1, nodes_per_batch));
+  if (chunk >= e->branches) chunk -= chunk % e->branches;
+  for (int b0 = 0; b0 < nbatch; b0 += chunk) {
+    cudaError_t rc = cudaStreamBeginCapture(e->cap, cudaStreamCaptureModeThreadLocal);
+    if (rc != cudaSuccess) {
+      destroy_graphs(ex);
+      return fail(SWIT_E_CUDA, "%s graph capture: %s", what, cudaGetErrorString(rc));
+    }
+    capture_fork(e);
+    for (int b = b0; b < std::min(nbatch, b0 + chunk); ++b) issue(b, capture_stream(e, b - b0));
+    capture_join(e);
+    cudaGraph_t graph = nullptr;
+    rc = cudaStreamEndCapture(e->cap, &graph);
+    if (rc != cudaSuccess) {
+      destroy_graphs(ex);
+      return fail(SWIT_E_CUDA, "%s graph capture: %s", what, cudaGetErrorString(rc));
+    }
+    cudaGraphExec_t x = nullptr;
+    rc = cudaGraphInstantiate(&x, graph, 0);
+    cudaGraphDestroy(graph);
+    if (rc != cudaSuccess) {
+      destroy_graphs(ex);
+      return fail(SWIT_E_CUDA, "%s graph instantiate: %s", what, cudaGetErrorString(rc));
+    }
+    ex.push_back(x);
+  }
+  return 0;
+}
+
+
 template <class R>
 int run_forward_loop(swit_engine* e, bool store, cudaStream_t st) {
   if (e->path == 1) {
@@ -598,31 +659,19 @@ int run_forward_loop(swit_engine* e, bool store, cudaStream_t st) {
     CK(cudaGetLastError());
     return 0;
   }
-  cudaGraphExec_t& ex = e->gfwd[store ? 1 : 0];
-  if (!ex) {
-    cudaGraph_t graph;
-    CK(cudaStreamBeginCapture(e->cap, cudaStreamCaptureModeThreadLocal));
-    const int fb = fwd_batch(e);
-    capture_fork(e);
-    for (int s0 = 0, b = 0; s0 < e->ns; s0 += fb, ++b) {
-      cudaStream_t cs = capture_stream(e, b);
+  std::vector<cudaGraphExec_t>& ex = e->gfwd[store ? 1 : 0];
+  if (ex.empty()) {
+    const int fb = fwd_batch(e), nbatch = (e->ns + fb - 1) / fb;
+    int rc = capture_chunked(e, ex, nbatch, loop_nodes(e), "forward", [&](int b, cudaStream_t cs) {
+      const int s0 = b * fb, nb = std::min(fb, e->ns - s0);
       if (store && e->ckpt_k)
-        forward_checkpointed<R>(e, s0, std::min(fb, e->ns - s0), cs);
+        forward_checkpointed<R>(e, s0, nb, cs);
       else
-        launch_forward_steps<R>(e, store, s0, std::min(fb, e->ns - s0), cs);
-    }
-    capture_join(e);
-    cudaError_t rc = cudaStreamEndCapture(e->cap, &graph);
-    if (rc != cudaSuccess) return fail(SWIT_E_CUDA, "forward graph capture: %s", cudaGetErrorString(rc));
-    rc = cudaGraphInstantiate(&ex, graph, 0);
-    cudaGraphDestroy(graph);
-    if (rc != cudaSuccess) {
-      ex = nullptr;
-      return fail(SWIT_E_CUDA, "forward graph instantiate: %s", cudaGetErrorString(rc));
-    }
+        launch_forward_steps<R>(e, store, s0, nb, cs);
+    });
+    if (rc) return rc;
   }
-  CK(cudaGraphLaunch(ex, st));
-  return 0;
+  return launch_graphs(ex, st);
 }
 
 template <class R>
@@ -637,29 +686,18 @@ int run_backward_loop(swit_engine* e, cudaStream_t st) {
     CK(cudaGetLastError());
     return 0;
   }
-  if (!e->gbwd) {
-    cudaGraph_t graph;
-    CK(cudaStreamBeginCapture(e->cap, cudaStreamCaptureModeThreadLocal));
-    capture_fork(e);
-    for (int s0 = 0, b = 0; s0 < e->ns; s0 += e->batch, ++b) {
-      cudaStream_t cs = capture_stream(e, b);
+  if (e->gbwd.empty()) {
+    const int nbatch = (e->ns + e->batch - 1) / e->batch;
+    int rc = capture_chunked(e, e->gbwd, nbatch, loop_nodes(e), "backward", [&](int b, cudaStream_t cs) {
+      const int s0 = b * e->batch, nb = std::min(e->batch, e->ns - s0);
       if (e->ckpt_k)
-        backward_checkpointed<R>(e, s0, std::min(e->batch, e->ns - s0), cs);
+        backward_checkpointed<R>(e, s0, nb, cs);
       else
-        launch_backward_steps<R>(e, s0, std::min(e->batch, e->ns - s0), cs);
-    }
-    capture_join(e);
-    cudaError_t rc = cudaStreamEndCapture(e->cap, &graph);
-    if (rc != cudaSuccess) return fail(SWIT_E_CUDA, "backward graph capture: %s", cudaGetErrorString(rc));
-    rc = cudaGraphInstantiate(&e->gbwd, graph, 0);
-    cudaGraphDestroy(graph);
-    if (rc != cudaSuccess) {
-      e->gbwd = nullptr;
-      return fail(SWIT_E_CUDA, "backward graph instantiate: %s", cudaGetErrorString(rc));
-    }
+        launch_backward_steps<R>(e, s0, nb, cs);
+    });
+    if (rc) return rc;
   }
-  CK(cudaGraphLaunch(e->gbwd, st));
-  return 0;
+  return launch_graphs(e->gbwd, st);
 }
 
 template <class R>
@@ -753,24 +791,14 @@ int run_exact_loop(swit_engine* e, cudaStream_t st) {
     CK(cudaGetLastError());
     return 0;
   }
-  if (!e->gxb) {
-    cudaGraph_t graph;
-    CK(cudaStreamBeginCapture(e->cap, cudaStreamCaptureModeThreadLocal));
-    capture_fork(e);
-    for (int s0 = 0, b = 0; s0 < e->ns; s0 += e->batch, ++b)
-      exact_reverse<R>(e, s0, std::min(e->batch, e->ns - s0), capture_stream(e, b));
-    capture_join(e);
-    cudaError_t rc = cudaStreamEndCapture(e->cap, &graph);
-    if (rc != cudaSuccess) return fail(SWIT_E_CUDA, "exact adjoint graph capture: %s", cudaGetErrorString(rc));
-    rc = cudaGraphInstantiate(&e->gxb, graph, 0);
-    cudaGraphDestroy(graph);
-    if (rc != cudaSuccess) {
-      e->gxb = nullptr;
-      return fail(SWIT_E_CUDA, "exact adjoint graph instantiate: %s", cudaGetErrorString(rc));
-    }
+  if (e->gxb.empty()) {
+    const int nbatch = (e->ns + e->batch - 1) / e->batch;
+    int rc = capture_chunked(e, e->gxb, nbatch, loop_nodes(e), "exact adjoint", [&](int b, cudaStream_t cs) {
+      exact_reverse<R>(e, b * e->batch, std::min(e->batch, e->ns - b * e->batch), cs);
+    });
+    if (rc) return rc;
   }
-  CK(cudaGraphLaunch(e->gxb, st));
-  return 0;
+  return launch_graphs(e->gxb, st);
 }
 
 // Exact adjoint after a storing forward run: adjoint sources already staged in
@@ -1703,7 +1731,10 @@ void auto_batches(swit_engine* e, int branches) {
   const int br = std::max(1, std::min(branches ? branches : 3, e->ns));
   const int per_branch = std::max(1, inflight / br);
   const int rounds = (e->ns + br * per_branch - 1) / (br * per_branch);
-  const int k = std::min(e->ns, br * rounds);
+  // and at most about 1 M kernel nodes per captured loop (grids whose state
+  // does not fit the L2 would otherwise run one shot per launch)
+  const int kmax = std::max(br, (int)(((size_t)1 << 20) / (2 * (size_t)(e->nt - 1))) / br * br);
+  const int k = std::min(std::min(e->ns, br * rounds), kmax);
   e->batch = (e->ns + k - 1) / k;
   e->branches = br;
 }
@@ -1808,6 +1839,11 @@ int swit_create(const swit_desc* d, swit_engine** out) {
                 d->graph_branches);
   }
   e->branches = d->graph_branches ? d->graph_branches : 2;
+  e->graph_nodes = kGraphNodes;
+  if (const char* gn = std::getenv("SWIT_GRAPH_NODES")) {  // smaller graphs, e.g. to test the chunking
+    const long long v = std::atoll(gn);
+    if (v > 0) e->graph_nodes = (size_t)v;
+  }
   if (d->shots_per_batch == 0 && e->path == 0 && e->variant == 3) auto_batches(e, d->graph_branches);
   e->ckpt_m = e->ckpt_k ? (e->nt + e->ckpt_k - 1) / e->ckpt_k : 0;
   e->snt = e->ckpt_k ? e->ckpt_k : e->nt;

@@ -196,3 +196,10 @@ def test_gradcheck_with_the_fp64_exact_adjoint():
 
         sv = src0.clone().requires_grad_(True)
         assert torch.autograd.gradcheck(f_src, (sv,), eps=2.0 ** -6, atol=1e-7, rtol=1e-4, fast_mode=True)
+
+
+def test_exact_loop_split_into_several_graphs(base, monkeypatch):
+    monkeypatch.setenv("SWIT_GRAPH_NODES", "1000")
+    _, g, gs = run(base, shots_per_batch=1)
+    np.testing.assert_array_equal(g, base["ref"]["g"])
+    np.testing.assert_array_equal(gs, base["ref"]["gsrc"])

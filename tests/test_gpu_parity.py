@@ -333,3 +333,21 @@ def test_kernel_profile_counts_launches_and_leaves_results_intact(base, opts, gr
         assert v["mean_ms"] > 0, k
     np.testing.assert_array_equal(seis, base["ref"]["seis"])
     np.testing.assert_array_equal(g, base["grad"]["g"])
+
+
+@pytest.mark.parametrize("opts", [dict(shots_per_batch=1), dict(shots_per_batch=1, graph_branches=2),
+                                  dict(shots_per_batch=1, checkpoint_every=40), dict(shots_per_batch=2)])
+def test_loops_split_into_several_graphs_give_the_same_bits(base, opts, monkeypatch):
+    """With a node bound of 1000 per graph every captured loop becomes one graph
+    per batch (or per round of branches); results stay the oracle's."""
+    monkeypatch.setenv("SWIT_GRAPH_NODES", "1000")
+    s = base["s"]
+    with engine(s, **opts) as e:
+        e.set_model(s.vp_true, base["rho"])
+        seis = e.forward(base["src"], save_boundary=True)
+        g, fw, bk = e.backward(base["adj"])
+        g2, _, _ = e.backward(base["adj"])
+    np.testing.assert_array_equal(seis, base["ref"]["seis"])
+    np.testing.assert_array_equal(g, base["grad"]["g"])
+    np.testing.assert_array_equal(g2, base["grad"]["g"])
+    np.testing.assert_array_equal(bk, base["grad"]["bk"])
