@@ -1,6 +1,6 @@
 // fd2d_oracle.cpp -- CPU oracle for the fd2dmpi forward / adjoint / imaging path.
 //
-// TEST INFRASTRUCTURE ONLY.  This file is the checker, never the product: only
+// TEST INFRASTRUCTURE ONLY.  This file checks results and is never the product: only
 // tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg may load it.
 // The GB300 engine (swit_gb300/csrc) never links or calls it.
 //
