@@ -574,18 +574,18 @@ void exact_reverse(swit_engine* e, int s0, int nb, cudaStream_t st) {
 // per branch (auto_batches): at 481x141, 127.6 shot-gradients/s with three
 // branches of 9-shot batches, 126.0 with two of 13, 105.3 with 13-shot batches
 // on three branches (one branch runs two batches) and 101.6 with one chain.
-inline cudaStream_t capture_stream(swit_engine* e, int b) {
+inline cudaStream_t capture_stream(swit_engine* e, int b, cudaStream_t origin) {
   const int k = b % e->branches;
-  return k ? e->capx[k - 1] : e->cap;
+  return k ? e->capx[k - 1] : origin;
 }
-inline void capture_fork(swit_engine* e) {
-  cudaEventRecord(e->ev_fork, e->cap);
+inline void capture_fork(swit_engine* e, cudaStream_t origin) {
+  cudaEventRecord(e->ev_fork, origin);
   for (int i = 0; i < e->branches - 1; ++i) cudaStreamWaitEvent(e->capx[i], e->ev_fork, 0);
 }
-inline void capture_join(swit_engine* e) {
+inline void capture_join(swit_engine* e, cudaStream_t origin) {
   for (int i = 0; i < e->branches - 1; ++i) {
     cudaEventRecord(e->ev_join[i], e->capx[i]);
-    cudaStreamWaitEvent(e->cap, e->ev_join[i], 0);
+    cudaStreamWaitEvent(origin, e->ev_join[i], 0);
   }
 }
 
@@ -625,9 +625,9 @@ int capture_chunked(swit_engine* e, std::vector<cudaGraphExec_t>& ex, int nbatch
       destroy_graphs(ex);
       return fail(SWIT_E_CUDA, "%s graph capture: %s", what, cudaGetErrorString(rc));
     }
-    capture_fork(e);
-    for (int b = b0; b < std::min(nbatch, b0 + chunk); ++b) issue(b, capture_stream(e, b - b0));
-    capture_join(e);
+    capture_fork(e, e->cap);
+    for (int b = b0; b < std::min(nbatch, b0 + chunk); ++b) issue(b, capture_stream(e, b - b0, e->cap));
+    capture_join(e, e->cap);
     cudaGraph_t graph = nullptr;
     rc = cudaStreamEndCapture(e->cap, &graph);
     if (rc != cudaSuccess) {
@@ -646,6 +646,23 @@ int capture_chunked(swit_engine* e, std::vector<cudaGraphExec_t>& ex, int nbatch
   return 0;
 }
 
+// True while the caller is capturing `st` into a graph of its own: the loops
+// are then issued straight onto st (the branches forked from and joined back
+// to it), since a graph launch cannot be captured.
+inline bool caller_capturing(cudaStream_t st) {
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  return cudaStreamIsCapturing(st, &cs) == cudaSuccess && cs == cudaStreamCaptureStatusActive;
+}
+
+template <class F>
+int issue_into_capture(swit_engine* e, cudaStream_t st, int nbatch, F&& issue) {
+  capture_fork(e, st);
+  for (int b = 0; b < nbatch; ++b) issue(b, capture_stream(e, b, st));
+  capture_join(e, st);
+  CK(cudaGetLastError());
+  return 0;
+}
+
 
 template <class R>
 int run_forward_loop(swit_engine* e, bool store, cudaStream_t st) {
@@ -660,15 +677,17 @@ int run_forward_loop(swit_engine* e, bool store, cudaStream_t st) {
     return 0;
   }
   std::vector<cudaGraphExec_t>& ex = e->gfwd[store ? 1 : 0];
+  const int fb = fwd_batch(e), nbatch = (e->ns + fb - 1) / fb;
+  auto issue = [&](int b, cudaStream_t cs) {
+    const int s0 = b * fb, nb = std::min(fb, e->ns - s0);
+    if (store && e->ckpt_k)
+      forward_checkpointed<R>(e, s0, nb, cs);
+    else
+      launch_forward_steps<R>(e, store, s0, nb, cs);
+  };
+  if (caller_capturing(st)) return issue_into_capture(e, st, nbatch, issue);
   if (ex.empty()) {
-    const int fb = fwd_batch(e), nbatch = (e->ns + fb - 1) / fb;
-    int rc = capture_chunked(e, ex, nbatch, loop_nodes(e), "forward", [&](int b, cudaStream_t cs) {
-      const int s0 = b * fb, nb = std::min(fb, e->ns - s0);
-      if (store && e->ckpt_k)
-        forward_checkpointed<R>(e, s0, nb, cs);
-      else
-        launch_forward_steps<R>(e, store, s0, nb, cs);
-    });
+    int rc = capture_chunked(e, ex, nbatch, loop_nodes(e), "forward", issue);
     if (rc) return rc;
   }
   return launch_graphs(ex, st);
@@ -686,15 +705,17 @@ int run_backward_loop(swit_engine* e, cudaStream_t st) {
     CK(cudaGetLastError());
     return 0;
   }
+  const int nbatch = (e->ns + e->batch - 1) / e->batch;
+  auto issue = [&](int b, cudaStream_t cs) {
+    const int s0 = b * e->batch, nb = std::min(e->batch, e->ns - s0);
+    if (e->ckpt_k)
+      backward_checkpointed<R>(e, s0, nb, cs);
+    else
+      launch_backward_steps<R>(e, s0, nb, cs);
+  };
+  if (caller_capturing(st)) return issue_into_capture(e, st, nbatch, issue);
   if (e->gbwd.empty()) {
-    const int nbatch = (e->ns + e->batch - 1) / e->batch;
-    int rc = capture_chunked(e, e->gbwd, nbatch, loop_nodes(e), "backward", [&](int b, cudaStream_t cs) {
-      const int s0 = b * e->batch, nb = std::min(e->batch, e->ns - s0);
-      if (e->ckpt_k)
-        backward_checkpointed<R>(e, s0, nb, cs);
-      else
-        launch_backward_steps<R>(e, s0, nb, cs);
-    });
+    int rc = capture_chunked(e, e->gbwd, nbatch, loop_nodes(e), "backward", issue);
     if (rc) return rc;
   }
   return launch_graphs(e->gbwd, st);
@@ -791,11 +812,13 @@ int run_exact_loop(swit_engine* e, cudaStream_t st) {
     CK(cudaGetLastError());
     return 0;
   }
+  const int nbatch = (e->ns + e->batch - 1) / e->batch;
+  auto issue = [&](int b, cudaStream_t cs) {
+    exact_reverse<R>(e, b * e->batch, std::min(e->batch, e->ns - b * e->batch), cs);
+  };
+  if (caller_capturing(st)) return issue_into_capture(e, st, nbatch, issue);
   if (e->gxb.empty()) {
-    const int nbatch = (e->ns + e->batch - 1) / e->batch;
-    int rc = capture_chunked(e, e->gxb, nbatch, loop_nodes(e), "exact adjoint", [&](int b, cudaStream_t cs) {
-      exact_reverse<R>(e, b * e->batch, std::min(e->batch, e->ns - b * e->batch), cs);
-    });
+    int rc = capture_chunked(e, e->gxb, nbatch, loop_nodes(e), "exact adjoint", issue);
     if (rc) return rc;
   }
   return launch_graphs(e->gxb, st);

@@ -351,3 +351,42 @@ def test_loops_split_into_several_graphs_give_the_same_bits(base, opts, monkeypa
     np.testing.assert_array_equal(g, base["grad"]["g"])
     np.testing.assert_array_equal(g2, base["grad"]["g"])
     np.testing.assert_array_equal(bk, base["grad"]["bk"])
+
+
+@pytest.mark.parametrize("adjoint", ["fd2dmpi", "exact"])
+def test_engine_calls_capture_into_a_cuda_graph(base, adjoint):
+    """With device buffers the C-ABI calls are stream-ordered with no host
+    synchronisation, so once an engine has built its own graphs a caller can
+    capture forward + backward into a graph of its own and replay it."""
+    import torch
+    s = base["s"]
+    with engine(s, adjoint=adjoint) as e:
+        e.set_model(torch.from_numpy(s.vp_true).cuda(), torch.from_numpy(base["rho"]).cuda())
+        src = torch.from_numpy(base["src"]).cuda()
+        adj = torch.from_numpy(base["adj"]).cuda()
+        seis = torch.zeros((s.ns, s.ng, s.nt), dtype=torch.float32, device="cuda")
+        g = torch.zeros((s.nx, s.nz), dtype=torch.float32, device="cuda")
+        fw, bk = torch.zeros_like(g), torch.zeros_like(g)
+
+        def step():
+            e.forward(src, save_boundary=True, seis=seis)
+            if adjoint == "exact":
+                e.backward_exact(adj, grad=g)
+            else:
+                e.backward(adj, grad=g, illum_fw=fw, illum_bk=bk)
+
+        step()  # builds the engine's graphs
+        torch.cuda.synchronize()
+        want_seis, want_g = seis.clone(), g.clone()
+        graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(graph, capture_error_mode="thread_local"):
+            step()
+        seis.zero_()
+        g.zero_()
+        for _ in range(2):
+            graph.replay()
+        torch.cuda.synchronize()
+    torch.testing.assert_close(seis, want_seis, rtol=0, atol=0)
+    torch.testing.assert_close(g, want_g, rtol=0, atol=0)
+    if adjoint == "fd2dmpi":
+        np.testing.assert_array_equal(g.cpu().numpy(), base["grad"]["g"])
