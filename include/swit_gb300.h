@@ -116,6 +116,10 @@ typedef struct swit_desc {
                                divergence term of every step, NX*LD values per
                                step and shot, or regenerates them segment by
                                segment with checkpoint_every: swit_backward_exact) */
+  int32_t receiver_component; /* 0 = pressure (fd2dmpi); 1 = vx, 2 = vz: the
+                               receivers record u or w and the adjoint source
+                               enters u or w (dev/solver/fdcore.f90:154-177,
+                               465-485; vec kernels, adjoint_mode 0)          */
 } swit_desc;
 
 /* Creates an engine and allocates its device workspace on the current device.

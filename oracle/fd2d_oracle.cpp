@@ -49,6 +49,7 @@ typedef struct oracle_desc {
   const float* zs;    // [ns]   source z (m)
   const float* xg;    // [ns*ngmax] receiver x (m)
   const float* zg;    // [ns*ngmax] receiver z (m)
+  int32_t comp;       // recorded component: 0 = p, 1 = vx (u), 2 = vz (w) (dev/solver/fdcore.f90:154-177)
 } oracle_desc;
 }
 
@@ -222,8 +223,10 @@ void forward_shot(const Setup<R>& S, const oracle_desc& d, int is, const float* 
     // fdcore.f90:116-120
     if (S.fs_flag == 1)
       for (int ix = 1; ix <= NX; ++ix) w(fs[ix] - 1, ix) = w(fs[ix], ix);
-    // fdcore.f90:123-128
-    for (int ig = 0; ig < ng; ++ig) seis[(size_t)ig * nt + (it - 1)] = p(gz[ig], gx[ig]);
+    // fdcore.f90:123-128; vx / vz receivers record u / w (dev/solver/fdcore.f90:154-177)
+    for (int ig = 0; ig < ng; ++ig)
+      seis[(size_t)ig * nt + (it - 1)] =
+          d.comp == 1 ? u(gz[ig], gx[ig]) : (d.comp == 2 ? w(gz[ig], gx[ig]) : p(gz[ig], gx[ig]));
     // fdcore.f90:130-159
     if (store) {
       R* b = boundary + (size_t)(it - 1) * SL;
@@ -416,10 +419,13 @@ void adjoint_shot(const Setup<R>& S, const oracle_desc& d, int is, const float* 
     for (int ig = 1; ig <= ng; ++ig) {
       R beta = dt;
       int igx = gx[ig - 1], igz = gz[ig - 1];
-      if (igz > fs[igx])
-        pb(igz, igx) = pb(igz, igx) + beta * sadj(it, ig);
+      const int z = igz > fs[igx] ? igz : fs[igx] + 1;
+      if (d.comp == 1)  // dev/solver/fdcore.f90:472-478
+        ub(z, igx) = ub(z, igx) - beta * sadj(it, ig);
+      else if (d.comp == 2)  // dev/solver/fdcore.f90:479-485
+        wb(z, igx) = wb(z, igx) - beta * sadj(it, ig);
       else
-        pb(fs[igx] + 1, igx) = pb(fs[igx] + 1, igx) + beta * sadj(it, ig);
+        pb(z, igx) = pb(z, igx) + beta * sadj(it, ig);
     }
     for (int ix = 1; ix <= NX; ++ix) pb(fs[ix] - 1, ix) = -pb(fs[ix] + 1, ix);
 
@@ -486,6 +492,7 @@ void run_ranks(int ns, int nthreads, F&& f) {
 int check_desc(const oracle_desc* d) {
   if (!d) return -1;
   if (d->nx < 8 || d->nz < 8 || d->npml < 2 || d->nt < 2 || d->ns < 1 || d->ngmax < 1) return -2;
+  if (d->comp < 0 || d->comp > 2) return -2;
   if (!(d->dx > 0.f) || !(d->dt > 0.f)) return -2;
   const int NX = d->nx + 2 * d->npml, NZ = d->nz + 2 * d->npml;
   auto gi = [&](float x) { return d->npml + (int)(x / d->dx) + 1; };
@@ -734,6 +741,7 @@ int exact_all(const oracle_desc* d, const float* vp, const float* rho, const flo
               R* gsrc, R* seis_out, int nthreads) {
   int rc = check_desc(d);
   if (rc) return rc;
+  if (d->comp != 0) return -2;  // pressure receivers only
   Setup<R> S;
   S.build(*d, vp, rho);
   const size_t N = (size_t)S.NX * S.NZ, NS = (size_t)d->ngmax * d->nt;

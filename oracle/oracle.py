@@ -28,7 +28,7 @@ class _Desc(C.Structure):
                 ("dx", C.c_float), ("dt", C.c_float), ("free_surface", C.c_int32),
                 ("ns", C.c_int32), ("ngmax", C.c_int32),
                 ("ng", C.POINTER(C.c_int32)), ("xs", C.POINTER(C.c_float)), ("zs", C.POINTER(C.c_float)),
-                ("xg", C.POINTER(C.c_float)), ("zg", C.POINTER(C.c_float))]
+                ("xg", C.POINTER(C.c_float)), ("zg", C.POINTER(C.c_float)), ("comp", C.c_int32)]
 
 
 _lib = None
@@ -48,7 +48,10 @@ def _p(a, ct=C.c_float):
 class Problem:
     """Model + acquisition in the units of SWIT's parfile and coord.txt."""
 
-    def __init__(self, nx, nz, npml, nt, dx, dt, src_xz, rec_xz, free_surface=1, ng=None):
+    def __init__(self, nx, nz, npml, nt, dx, dt, src_xz, rec_xz, free_surface=1, ng=None, comp="p"):
+        if comp not in ("p", "vx", "vz"):
+            raise ValueError("comp must be 'p', 'vx' or 'vz'")
+        self.comp = {"p": 0, "vx": 1, "vz": 2}[comp]
         self.nx, self.nz, self.npml, self.nt = int(nx), int(nz), int(npml), int(nt)
         self.dx, self.dt = np.float32(dx), np.float32(dt)
         self.free_surface = int(free_surface)
@@ -66,7 +69,7 @@ class Problem:
 
     def desc(self):
         d = _Desc(self.nx, self.nz, self.npml, self.nt, self.dx, self.dt, self.free_surface, self.ns, self.ngmax,
-                  _p(self.ng, C.c_int32), _p(self.xs), _p(self.zs), _p(self.xg), _p(self.zg))
+                  _p(self.ng, C.c_int32), _p(self.xs), _p(self.zs), _p(self.xg), _p(self.zg), self.comp)
         return d
 
     @property

@@ -27,7 +27,7 @@ class SwitDesc(C.Structure):
                 ("rec_x", C.c_void_p), ("rec_z", C.c_void_p), ("precision", C.c_int32), ("path", C.c_int32),
                 ("shots_per_batch", C.c_int32), ("block_x", C.c_int32),
                 ("kernel_variant", C.c_int32), ("checkpoint_every", C.c_int32),
-                ("graph_branches", C.c_int32), ("adjoint_mode", C.c_int32)]
+                ("graph_branches", C.c_int32), ("adjoint_mode", C.c_int32), ("receiver_component", C.c_int32)]
 
 
 class SwitError(RuntimeError):

@@ -120,6 +120,7 @@ struct swit_engine {
   // exact discrete adjoint (adjoint_mode 1, kernels_exact.cuh): the strip buffer holds the forward's D of
   // every step (SL = NX * LD); mirror rows, source gradient, dA/dc; graph of its reverse loop
   int exact = 0;
+  int rcomp = 0;  // recorded component: 0 = p, 1 = vx, 2 = vz (swit_desc.receiver_component)
   void *xm = nullptr, *xsrc = nullptr, *xdadc = nullptr;
   std::vector<cudaGraphExec_t> gxb;
   size_t graph_nodes = 0;  // node bound per captured graph (kGraphNodes; SWIT_GRAPH_NODES overrides)
@@ -204,7 +205,7 @@ Grid<R> make_grid(const swit_engine* e) {
 }
 
 inline Receivers make_rec(const swit_engine* e) {
-  return Receivers{e->d_colptr, e->d_ig, e->d_zr, e->d_zlo, e->d_zhi};
+  return Receivers{e->d_colptr, e->d_ig, e->d_zr, e->d_zlo, e->d_zhi, e->rcomp};
 }
 inline Sources make_src(const swit_engine* e) { return Sources{e->d_isx, e->d_isz, e->d_risx, e->d_risz}; }
 
@@ -439,6 +440,9 @@ void launch_backward_steps(swit_engine* e, int shot0, int nb, cudaStream_t st, i
       launch_pdl(e->pdl, k_bwd_p_v<R>, g3, block, st, g, l3, make_rec(e), make_src(e), (const R*)e->src,
                  (const R*)e->adj_t, (R*)e->pb, (const R*)e->ub, (const R*)e->wb, (R*)e->pe, (const R*)e->ue,
                  (const R*)e->we, (R*)e->dg, (R*)e->dfw, (R*)e->dbk, (const R*)e->strips, it, shot0);
+      if (e->rcomp)  // vx / vz receivers: adjoint source into u / w
+        launch_pdl(e->pdl, k_inject_vel<R>, dim3((e->NX + 255) / 256, nb), dim3(256), st, g, make_rec(e),
+                   (const R*)e->adj_t, (R*)e->ub, (R*)e->wb, it, shot0);
     }
     return;
   }
@@ -1809,6 +1813,15 @@ int swit_create(const swit_desc* d, swit_engine** out) {
     return fail(SWIT_E_ARG, "the exact adjoint runs on the vec kernels (kernel_variant 0 or 3)");
   }
   e->exact = d->adjoint_mode;
+  if (d->receiver_component < 0 || d->receiver_component > 2) {
+    delete e;
+    return fail(SWIT_E_ARG, "receiver_component must be 0 (p), 1 (vx) or 2 (vz) (got %d)", d->receiver_component);
+  }
+  if (d->receiver_component && (e->variant != 3 || e->exact)) {
+    delete e;
+    return fail(SWIT_E_ARG, "vx / vz receivers run on the vec kernels with fd2dmpi's adjoint (adjoint_mode 0)");
+  }
+  e->rcomp = d->receiver_component;
   if (e->exact) e->SL = e->NX * e->LD;  // the strip buffer holds D of each step
   if (e->variant == 2 && e->LD > 1024) {
     delete e;
@@ -2204,7 +2217,7 @@ int swit_multi_create(const swit_desc* descs, int32_t n, swit_multi** out) {
     const swit_desc& d = descs[i];
     if (d.nx + 2 * d.npml > 16384 || d.ns > 65535) return fail(SWIT_E_LIMIT, "instance %d: more than 16384 PML-grid columns", i);
     if (d.precision != 0 || d.path != 0 || (d.kernel_variant != 0 && d.kernel_variant != 3) || d.checkpoint_every ||
-        d.adjoint_mode)
+        d.adjoint_mode || d.receiver_component)
       return fail(SWIT_E_ARG,
                   "instance %d: a multi-instance engine runs FP32 vec kernels on the batched path with boundary saving",
                   i);

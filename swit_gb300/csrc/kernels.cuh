@@ -50,6 +50,7 @@ struct Receivers {
   const int* __restrict__ zrow;
   const int* __restrict__ zlo;  // per shot: lowest and highest receiver row (vectorised kernels;
   const int* __restrict__ zhi;  // may be null elsewhere)
+  int comp;                     // recorded component: 0 = p, 1 = vx (u), 2 = vz (w); vec kernels only
 };
 
 struct Sources {

@@ -371,7 +371,10 @@ __device__ __forceinline__ void fwd_uw_body(const Grid<R>& g, const Receivers& r
     const int e1 = cp[ix + 1];
     for (int e = cp[ix]; e < e1; ++e) {
       const int j = rec.zrow[e] - iz0;
-      if (j >= 0 && j < 4) seis_t[((size_t)v.s * g.nt + (it - 1)) * g.ngmax + rec.ig[e]] = p0.x[j];
+      // vx / vz receivers record u / w after their update (dev/solver/fdcore.f90:162-175)
+      if (j >= 0 && j < 4)
+        seis_t[((size_t)v.s * g.nt + (it - 1)) * g.ngmax + rec.ig[e]] =
+            rec.comp == 1 ? uv.x[j] : (rec.comp == 2 ? wv.x[j] : p0.x[j]);
     }
   }
   // boundary strips of step it (fdcore.f90:130-159)
@@ -580,7 +583,7 @@ __device__ __forceinline__ void bwd_p_body(const Grid<R>& g, const Receivers& re
   if (!CHK) {
     st4(pb, v.k4, pv);
   } else {
-    if (iz0 + 3 >= rec.zlo[v.s] && iz0 <= rec.zhi[v.s]) {
+    if (rec.comp == 0 && iz0 + 3 >= rec.zlo[v.s] && iz0 <= rec.zhi[v.s]) {
       const int* cp = rec.colptr + (size_t)v.s * (NX + 2);
       const int e1 = cp[ix + 1];
       for (int e = cp[ix]; e < e1; ++e) {
@@ -681,6 +684,27 @@ __global__ void __launch_bounds__(256, SWIT_VEC_MINB_R(R)) k_bwd_p_v(Grid<R> g, 
 // bwd_p), the highest any shot needs; 3 where the phase does no work: rows
 // above fs-1 in the forward (no update, mirror, source, receiver or strip
 // there) and rows from NZ on.  out[k * NX * LD/4 + (ix-1) * LD/4 + q].
+// vx / vz receivers: after the adjoint pressure phase of reverse step it, the
+// adjoint source of step it goes into u or w at the receiver point
+// (dev/solver/fdcore.f90:472-485: u(z, igx) = u(z, igx) - dt s(it, ig)), in
+// receiver order; one thread per column and shot.
+template <class R>
+__global__ void k_inject_vel(Grid<R> g, Receivers rec, const R* __restrict__ adj_t, R* UB, R* WB, int it,
+                             int shot0) {
+  const int ix = blockIdx.x * blockDim.x + threadIdx.x + 1;
+  const int s = shot0 + blockIdx.y;
+  pdl_enter();
+  if (ix > g.NX) return;
+  const int* cp = rec.colptr + (size_t)s * (g.NX + 2);
+  const int e1 = cp[ix + 1];
+  if (cp[ix] == e1) return;
+  R* f = (rec.comp == 1 ? UB : WB) + (size_t)s * g.FSZ + (size_t)(ix - 1) * g.LD;
+  for (int e = cp[ix]; e < e1; ++e) {
+    const int z = rec.zrow[e];
+    f[z - 1] = f[z - 1] - g.dt * adj_t[((size_t)s * g.nt + (it - 1)) * g.ngmax + rec.ig[e]];
+  }
+}
+
 template <class R>
 __global__ void k_tiers(Grid<R> g, Sources src, Receivers rec, int ns, int* out) {
   const int LD4 = g.LD >> 2;

@@ -28,7 +28,7 @@ class Engine:
 
     def __init__(self, nx, nz, npml, nt, dx, dt, src_xz, rec_xz, free_surface=1, ng=None, precision="fp32",
                  path="batched", shots_per_batch=0, block_x=0, kernel="auto", checkpoint_every=0, graph_branches=0,
-                 adjoint="fd2dmpi", _borrow=None):
+                 adjoint="fd2dmpi", receiver_component="p", _borrow=None):
         lib = _lib.load()
         src_xz = np.asarray(src_xz, dtype=np.float32).reshape(-1, 2)
         rec_xz = np.asarray(rec_xz, dtype=np.float32)
@@ -50,6 +50,10 @@ class Engine:
         if adjoint not in ("fd2dmpi", "exact"):
             raise ValueError("adjoint must be 'fd2dmpi' or 'exact'")
         self.adjoint = adjoint
+        comps = {"p": 0, "vx": 1, "vz": 2}
+        if receiver_component not in comps:
+            raise ValueError("receiver_component must be 'p', 'vx' or 'vz'")
+        self.receiver_component = receiver_component
         if kernel not in variants:
             raise ValueError("kernel must be one of %s" % ", ".join(sorted(variants)))
         self._keep = dict(
@@ -61,7 +65,8 @@ class Engine:
                           self.ngmax, k["ng"].ctypes.data, k["xs"].ctypes.data, k["zs"].ctypes.data,
                           k["xg"].ctypes.data, k["zg"].ctypes.data, 1 if self.fp64 else 0,
                           1 if path == "plain" else 0, int(shots_per_batch), int(block_x), variants[kernel],
-                          int(checkpoint_every), int(graph_branches), 1 if adjoint == "exact" else 0)
+                          int(checkpoint_every), int(graph_branches), 1 if adjoint == "exact" else 0,
+                          comps[receiver_component])
         self.checkpoint_every = int(checkpoint_every)
         self._desc = d
         self._lib = lib

@@ -390,3 +390,37 @@ def test_engine_calls_capture_into_a_cuda_graph(base, adjoint):
     torch.testing.assert_close(g, want_g, rtol=0, atol=0)
     if adjoint == "fd2dmpi":
         np.testing.assert_array_equal(g.cpu().numpy(), base["grad"]["g"])
+
+
+@pytest.fixture(scope="module")
+def vel():
+    """Oracle runs with vx and vz receivers (dev/solver/fdcore.f90:154-177, 465-485)."""
+    s = survey.small()
+    src = s.source()
+    rho = s.rho(s.vp_true)
+    out = {}
+    for comp in ("vx", "vz"):
+        pb = O.Problem(s.nx, s.nz, s.npml, s.nt, s.dx, s.dt, s.src_xz, s.rec_xz, free_surface=s.free_surface,
+                       comp=comp)
+        ref = O.forward(pb, s.vp_true, rho, src, store=True)
+        adj = (ref["seis"] * 1e3).astype(np.float32)
+        out[comp] = dict(ref=ref, adj=adj, grad=O.adjoint(pb, s.vp_true, rho, src, adj, ref))
+    return dict(s=s, src=src, rho=rho, out=out)
+
+
+@pytest.mark.parametrize("comp", ["vx", "vz"])
+@pytest.mark.parametrize("opts", [dict(), dict(path="plain"), dict(shots_per_batch=1, graph_branches=3),
+                                  dict(checkpoint_every=40), dict(precision="fp64")])
+def test_velocity_receivers_match_oracle(vel, comp, opts):
+    s, o = vel["s"], vel["out"][comp]
+    with engine(s, kernel="vec", receiver_component=comp, **opts) as e:
+        e.set_model(s.vp_true, vel["rho"])
+        seis = e.forward(vel["src"], save_boundary=True)
+        g, fw, bk = e.backward(o["adj"])
+    if opts.get("precision") == "fp64":
+        assert rel(seis, o["ref"]["seis"]) <= SEIS_TOL and rel(g, o["grad"]["g"]) <= GRAD_TOL
+        return
+    np.testing.assert_array_equal(seis, o["ref"]["seis"])
+    np.testing.assert_array_equal(g, o["grad"]["g"])
+    np.testing.assert_array_equal(fw, o["grad"]["fw"])
+    np.testing.assert_array_equal(bk, o["grad"]["bk"])

@@ -125,3 +125,41 @@ def test_oracle_rejects_sources_outside_the_model():
     pb.xs[0] = 1e6
     with pytest.raises(ValueError):
         O.forward(pb, s.vp_true, s.rho(s.vp_true), s.source(), store=False)
+
+
+def test_velocity_receivers_record_u_and_w():
+    """vx / vz receivers (dev/solver/fdcore.f90:154-177) record u or w at the
+    receiver points; the wavefield itself, and so the strips, do not change.
+    Their adjoint source enters u or w (465-485): a zero source gives a zero
+    gradient, a non-zero one a gradient different from the pressure one."""
+    s = survey.small(nt=200)
+    rho = s.rho(s.vp_true)
+    src = s.source()
+    out = {}
+    for comp in ("p", "vx", "vz"):
+        pb = O.Problem(s.nx, s.nz, s.npml, s.nt, s.dx, s.dt, s.src_xz, s.rec_xz, comp=comp)
+        out[comp] = O.forward(pb, s.vp_true, rho, src, store=True)
+    for comp in ("vx", "vz"):
+        np.testing.assert_array_equal(out[comp]["boundary"], out["p"]["boundary"])
+        assert np.abs(out[comp]["seis"]).max() > 0
+        assert not np.array_equal(out[comp]["seis"], out["p"]["seis"])
+    assert not np.array_equal(out["vx"]["seis"], out["vz"]["seis"])
+    # the last sample of each trace is the field at the receiver point after the last step
+    L = s.npml
+    for comp, key in (("p", "p_end"), ("vx", "u_end"), ("vz", "w_end")):
+        for i in range(s.ns):
+            for ig in range(s.ng):
+                jx = int(np.float32(s.rec_xz[i, ig, 0]) / np.float32(s.dx)) + 1
+                jz = int(np.float32(s.rec_xz[i, ig, 1]) / np.float32(s.dx)) + 1
+                jz = jz + 1 if jz + L == L + 1 else jz  # a receiver on the free surface moves one node down
+                assert out[comp]["seis"][i, ig, -1] == out["p"][key][i, jx - 1, jz - 1]
+    g = {}
+    for comp in ("p", "vx"):
+        pb = O.Problem(s.nx, s.nz, s.npml, s.nt, s.dx, s.dt, s.src_xz, s.rec_xz, comp=comp)
+        zero = np.zeros_like(out[comp]["seis"], dtype=np.float32)
+        assert not O.adjoint(pb, s.vp_true, rho, src, zero, out[comp])["g"].any()
+        g[comp] = O.adjoint(pb, s.vp_true, rho, src, out[comp]["seis"].astype(np.float32), out[comp])["g"]
+        assert np.abs(g[comp]).max() > 0
+    assert not np.array_equal(g["p"], g["vx"])
+    with pytest.raises(ValueError):
+        O.Problem(s.nx, s.nz, s.npml, s.nt, s.dx, s.dt, s.src_xz, s.rec_xz, comp="vy")
