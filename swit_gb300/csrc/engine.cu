@@ -1593,21 +1593,36 @@ struct swit_multi {
   int max_nt = 0;
   Inst<float>* d_tab = nullptr;
   uint32_t* d_list[4] = {nullptr, nullptr, nullptr, nullptr};
-  uint2* d_blocks[4] = {nullptr, nullptr, nullptr, nullptr};
-  int* d_on = nullptr;      // per table row: instance switched on for this call
-  std::vector<int> act[4];  // active blocks: [k][s] at forward step s (k = 0, 1) or reverse index s (k = 2, 3)
-  cudaStream_t cap = nullptr;
-  cudaGraphExec_t gf[2] = {nullptr, nullptr};
-  cudaGraphExec_t gb = nullptr;
+  uint2* d_blocks[4] = {nullptr, nullptr, nullptr, nullptr};  // the waves' block tables, one after another
+  int* d_on = nullptr;  // per table row: instance switched on for this call
+  // A wave is a group of (instance, shot) pairs, in table order, whose reverse-loop state fits its share of
+  // the L2; waves run their loops on concurrent graph branches.  act[k][s]: active blocks of kernel k at forward
+  // step s (k = 0, 1) or reverse index s (k = 2, 3).
+  struct Wave {
+    int max_nt = 0;
+    size_t boff[4] = {0, 0, 0, 0};
+    std::vector<int> act[4];
+    std::vector<int> rows;         // table rows with a pair in this wave
+    cudaGraphExec_t g[3] = {nullptr, nullptr, nullptr};  // its forward (no strips, strips) and reverse loops
+  };
+  std::vector<Wave> waves;
+  int branches = 3;
+  cudaStream_t cap = nullptr, capx[2] = {nullptr, nullptr};
+  cudaEvent_t ev_fork = nullptr, ev_join[2] = {nullptr, nullptr};
 };
 
 namespace {
 
 void multi_release(swit_multi* m) {
-  for (int i = 0; i < 2; ++i)
-    if (m->gf[i]) cudaGraphExecDestroy(m->gf[i]);
-  if (m->gb) cudaGraphExecDestroy(m->gb);
+  for (auto& w : m->waves)
+    for (cudaGraphExec_t& x : w.g)
+      if (x) cudaGraphExecDestroy(x);
   if (m->cap) cudaStreamDestroy(m->cap);
+  for (int i = 0; i < 2; ++i) {
+    if (m->capx[i]) cudaStreamDestroy(m->capx[i]);
+    if (m->ev_join[i]) cudaEventDestroy(m->ev_join[i]);
+  }
+  if (m->ev_fork) cudaEventDestroy(m->ev_fork);
   if (m->d_tab) cudaFree(m->d_tab);
   if (m->d_on) cudaFree(m->d_on);
   for (int k = 0; k < 4; ++k) {
@@ -1620,7 +1635,11 @@ void multi_release(swit_multi* m) {
   }
 }
 
-// Instance table, padded task lists, block tables and active prefixes.
+// Instance table, padded task lists, waves with their block tables and active
+// prefixes.  Waves take (instance, shot) pairs in table order (record length,
+// longest first) while their reverse-loop state stays under 0.7 L2 / branches
+// (as the single-instance engine sizes its batches), at most about 1 M kernel
+// nodes per loop over all waves.
 int multi_build(swit_multi* m) {
   const int n = (int)m->eng.size();
   m->order.resize(n);
@@ -1655,81 +1674,160 @@ int multi_build(swit_multi* m) {
   CK(cudaMalloc(&m->d_tab, n * sizeof(Inst<float>)));
   CK(cudaMemcpy(m->d_tab, tab.data(), n * sizeof(Inst<float>), cudaMemcpyHostToDevice));
   CK(cudaMalloc(&m->d_on, n * sizeof(int)));
+  // padded task lists of every instance, one array per kernel
+  std::vector<uint32_t> base[4], chunks[4];
   for (int k = 0; k < 4; ++k) {
     std::vector<uint32_t> L;
-    std::vector<uint2> B;
-    std::vector<int> cum(n);
     for (int r = 0; r < n; ++r) {
       const swit_engine* e = m->eng[m->order[r]];
       const uint32_t* src = &e->h_list[(size_t)k * e->list_stride];
-      const uint32_t base = (uint32_t)L.size();
+      base[k].push_back((uint32_t)L.size());
       for (int i = 0; i < e->list_len[k]; ++i) {
         const uint32_t t = i < e->list_n0[k] ? 0u : (i < e->list_n1[k] ? 1u : 2u);
         L.push_back((t << 30) | src[i]);
       }
       while (L.size() % 256) L.push_back(kMultiPad);
-      const int chunks = (int)((L.size() - base) / 256);
-      for (int s = 0; s < e->ns; ++s)
-        for (int c = 0; c < chunks; ++c) B.push_back(make_uint2(((uint32_t)r << 16) | (uint32_t)s, base + 256u * c));
-      cum[r] = (int)B.size();
+      chunks[k].push_back((uint32_t)((L.size() - base[k][r]) / 256));
     }
     CK(cudaMalloc(&m->d_list[k], std::max<size_t>(L.size(), 1) * sizeof(uint32_t)));
     CK(cudaMemcpy(m->d_list[k], L.data(), L.size() * sizeof(uint32_t), cudaMemcpyHostToDevice));
-    CK(cudaMalloc(&m->d_blocks[k], std::max<size_t>(B.size(), 1) * sizeof(uint2)));
-    CK(cudaMemcpy(m->d_blocks[k], B.data(), B.size() * sizeof(uint2), cudaMemcpyHostToDevice));
-    // instances with nt >= s run forward step s and reverse index s - 2: a prefix of the order
-    m->act[k].assign(m->max_nt + 1, 0);
-    for (int s = 2; s <= m->max_nt; ++s) {
-      int nr = 0;
-      while (nr < n && m->eng[m->order[nr]]->nt >= s) ++nr;
-      const int a = nr ? cum[nr - 1] : 0;
-      if (k < 2)
-        m->act[k][s] = a;
-      else
-        m->act[k][s - 2] = a;
-    }
   }
+  // waves of (row, shot) pairs
+  int dev = 0, l2 = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, dev) != cudaSuccess ||
+      l2 <= 0)
+    l2 = 64 << 20;
+  std::vector<double> state(n);
+  for (int r = 0; r < n; ++r) {
+    const swit_engine* e = m->eng[m->order[r]];
+    state[r] = (3.0 * e->NX * e->NZ + 6.0 * e->nx * e->nz) * sizeof(float);
+  }
+  double budget = 0.7 * l2 / m->branches;
+  if (const char* wb = std::getenv("SWIT_MULTI_WAVE_BYTES")) {  // smaller waves, e.g. to test them
+    const double v = std::atof(wb);
+    if (v > 0) budget = v;
+  }
+  std::vector<std::vector<std::pair<int, int>>> groups;
+  for (int attempt = 0; attempt < 64; ++attempt) {
+    groups.clear();
+    double used = 0.0;
+    for (int r = 0; r < n; ++r)
+      for (int sh = 0; sh < m->eng[m->order[r]]->ns; ++sh) {
+        if (groups.empty() || (used + state[r] > budget && !groups.back().empty())) {
+          groups.emplace_back();
+          used = 0.0;
+        }
+        groups.back().emplace_back(r, sh);
+        used += state[r];
+      }
+    size_t nodes = 0;
+    for (auto& gr : groups) nodes += 2 * (size_t)(m->eng[m->order[gr.front().first]]->nt - 1);
+    if (nodes <= ((size_t)1 << 20) || groups.size() <= (size_t)m->branches) break;
+    budget *= 1.5;
+  }
+  std::vector<uint2> B[4];
+  for (auto& gr : groups) {
+    swit_multi::Wave w;
+    w.max_nt = m->eng[m->order[gr.front().first]]->nt;
+    for (auto& pr : gr)
+      if (w.rows.empty() || w.rows.back() != pr.first) w.rows.push_back(pr.first);
+    for (int k = 0; k < 4; ++k) {
+      w.boff[k] = B[k].size();
+      std::vector<int> cum;  // blocks up to and including each pair
+      for (auto& pr : gr) {
+        const int r = pr.first;
+        for (uint32_t c = 0; c < chunks[k][r]; ++c)
+          B[k].push_back(make_uint2(((uint32_t)r << 16) | (uint32_t)pr.second, base[k][r] + 256u * c));
+        cum.push_back((int)(B[k].size() - w.boff[k]));
+      }
+      // pairs whose instance has nt >= s run forward step s and reverse index s - 2: a prefix of the wave
+      w.act[k].assign(w.max_nt + 1, 0);
+      for (int s = 2; s <= w.max_nt; ++s) {
+        size_t np = 0;
+        while (np < gr.size() && m->eng[m->order[gr[np].first]]->nt >= s) ++np;
+        const int a = np ? cum[np - 1] : 0;
+        if (k < 2)
+          w.act[k][s] = a;
+        else
+          w.act[k][s - 2] = a;
+      }
+    }
+    m->waves.push_back(std::move(w));
+  }
+  for (int k = 0; k < 4; ++k) {
+    CK(cudaMalloc(&m->d_blocks[k], std::max<size_t>(B[k].size(), 1) * sizeof(uint2)));
+    CK(cudaMemcpy(m->d_blocks[k], B[k].data(), B[k].size() * sizeof(uint2), cudaMemcpyHostToDevice));
+  }
+  m->branches = std::max(1, std::min(m->branches, (int)m->waves.size()));
   CK(cudaStreamCreateWithFlags(&m->cap, cudaStreamNonBlocking));
+  for (int i = 0; i < 2; ++i) {
+    CK(cudaStreamCreateWithFlags(&m->capx[i], cudaStreamNonBlocking));
+    CK(cudaEventCreateWithFlags(&m->ev_join[i], cudaEventDisableTiming));
+  }
+  CK(cudaEventCreateWithFlags(&m->ev_fork, cudaEventDisableTiming));
   return 0;
 }
 
 // The forward (which = 0: no strips, 1: with strips) or reverse (which = 2)
-// loop of every switched-on instance, one launch per phase and step, captured
-// once.  on[i] (caller order) switches instance i on for this call.
+// loop of every switched-on instance.  Each wave's loop (one launch per phase
+// and step) is captured once into a graph of its own; a call launches the
+// graphs of the waves that hold a switched-on instance, spread over the
+// concurrent branch streams.  on[i] (caller order) switches instance i on.
 int multi_loop(swit_multi* m, int which, const std::vector<int>& on, cudaStream_t st) {
   std::vector<int> rows(m->eng.size());
   for (size_t r = 0; r < rows.size(); ++r) rows[r] = on[m->order[r]];
   CK(cudaMemcpyAsync(m->d_on, rows.data(), rows.size() * sizeof(int), cudaMemcpyHostToDevice, st));
-  cudaGraphExec_t& ex = which == 2 ? m->gb : m->gf[which];
-  if (!ex) {
-    cudaGraph_t graph;
-    CK(cudaStreamBeginCapture(m->cap, cudaStreamCaptureModeThreadLocal));
-    const dim3 block(256);
-    const Inst<float>* tab = m->d_tab;
-    auto ml = [&](int k, int nb) { return MultiLaunch{m->d_blocks[k], m->d_list[k], m->d_on, nb}; };
-    auto grid = [](int nb) { return dim3((unsigned)std::max(1, nb)); };
+  const dim3 block(256);
+  const Inst<float>* tab = m->d_tab;
+  auto grid = [](int nb) { return dim3((unsigned)std::max(1, nb)); };
+  std::vector<int> active;
+  for (int wi = 0; wi < (int)m->waves.size(); ++wi)
+    for (int r : m->waves[wi].rows)
+      if (rows[r]) {
+        active.push_back(wi);
+        break;
+      }
+  for (int wi : active) {
+    swit_multi::Wave& w = m->waves[wi];
+    if (w.g[which]) continue;
+    cudaError_t rc = cudaStreamBeginCapture(m->cap, cudaStreamCaptureModeThreadLocal);
+    if (rc != cudaSuccess) return fail(SWIT_E_CUDA, "multi-instance graph capture: %s", cudaGetErrorString(rc));
+    auto ml = [&](int k, int nb) { return MultiLaunch{m->d_blocks[k] + w.boff[k], m->d_list[k], m->d_on, nb}; };
     if (which < 2) {
-      for (int it = 2; it <= m->max_nt; ++it) {
-        launch_pdl(true, k_fwd_p_m<float>, grid(m->act[0][it]), block, m->cap, tab, ml(0, m->act[0][it]), it);
-        launch_pdl(true, k_fwd_uw_m<float>, grid(m->act[1][it]), block, m->cap, tab, ml(1, m->act[1][it]), it,
+      for (int it = 2; it <= w.max_nt; ++it) {
+        launch_pdl(true, k_fwd_p_m<float>, grid(w.act[0][it]), block, m->cap, tab, ml(0, w.act[0][it]), it);
+        launch_pdl(true, k_fwd_uw_m<float>, grid(w.act[1][it]), block, m->cap, tab, ml(1, w.act[1][it]), it,
                    which);
       }
     } else {
-      for (int jr = 0; jr <= m->max_nt - 2; ++jr) {
-        launch_pdl(true, k_bwd_uw_m<float>, grid(m->act[2][jr]), block, m->cap, tab, ml(2, m->act[2][jr]), jr);
-        launch_pdl(true, k_bwd_p_m<float>, grid(m->act[3][jr]), block, m->cap, tab, ml(3, m->act[3][jr]), jr);
+      for (int jr = 0; jr <= w.max_nt - 2; ++jr) {
+        launch_pdl(true, k_bwd_uw_m<float>, grid(w.act[2][jr]), block, m->cap, tab, ml(2, w.act[2][jr]), jr);
+        launch_pdl(true, k_bwd_p_m<float>, grid(w.act[3][jr]), block, m->cap, tab, ml(3, w.act[3][jr]), jr);
       }
     }
-    cudaError_t rc = cudaStreamEndCapture(m->cap, &graph);
-    if (rc != cudaSuccess) return fail(SWIT_E_CUDA, "multi-instance graph capture: %s", cudaGetErrorString(rc));
-    rc = cudaGraphInstantiate(&ex, graph, 0);
-    cudaGraphDestroy(graph);
+    cudaGraph_t graph = nullptr;
+    rc = cudaStreamEndCapture(m->cap, &graph);
+    if (rc == cudaSuccess) {
+      rc = cudaGraphInstantiate(&w.g[which], graph, 0);
+      cudaGraphDestroy(graph);
+    }
     if (rc != cudaSuccess) {
-      ex = nullptr;
-      return fail(SWIT_E_CUDA, "multi-instance graph instantiate: %s", cudaGetErrorString(rc));
+      w.g[which] = nullptr;
+      return fail(SWIT_E_CUDA, "multi-instance graph: %s", cudaGetErrorString(rc));
     }
   }
-  CK(cudaGraphLaunch(ex, st));
+  // the waves on the branch streams, forked from and joined back to st
+  const int br = std::max(1, std::min(m->branches, (int)active.size()));
+  CK(cudaEventRecord(m->ev_fork, st));
+  for (int i = 0; i < br - 1; ++i) CK(cudaStreamWaitEvent(m->capx[i], m->ev_fork, 0));
+  for (size_t k = 0; k < active.size(); ++k) {
+    const int b = (int)(k % br);
+    CK(cudaGraphLaunch(m->waves[active[k]].g[which], b ? m->capx[b - 1] : st));
+  }
+  for (int i = 0; i < br - 1; ++i) {
+    CK(cudaEventRecord(m->ev_join[i], m->capx[i]));
+    CK(cudaStreamWaitEvent(st, m->ev_join[i], 0));
+  }
   return 0;
 }
 

@@ -164,11 +164,16 @@ def _uneven_problems():
     return out
 
 
-def test_multi_engine_matches_each_engine_bit_for_bit():
+@pytest.mark.parametrize("wave_bytes", [None, "1", "3e6"])
+def test_multi_engine_matches_each_engine_bit_for_bit(wave_bytes, monkeypatch):
     """All problems stepped by shared launches give each problem's own engine's
-    seismogram misfit, gradient and illuminations exactly, twice in a row."""
+    seismogram misfit, gradient and illuminations exactly, twice in a row; also
+    with one (problem, shot) pair per wave on the concurrent branches, and with
+    waves of a few pairs."""
     import torch
     from swit_gb300 import MultiEngine
+    if wave_bytes:
+        monkeypatch.setenv("SWIT_MULTI_WAVE_BYTES", wave_bytes)
     surveys = _uneven_problems()
     ref = []
     for s in surveys:
