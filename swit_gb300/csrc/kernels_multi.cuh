@@ -4,11 +4,12 @@
 // Each instance is a regular engine (its own arrays); a device table holds per
 // instance the grid description, receiver and source tables and array
 // pointers.  Per phase kernel, every instance's own task list (kernels_vec.cuh)
-// is padded to whole blocks of 256 entries and the blocks of all instances and
-// shots are listed in a block table, instances ordered by record length nt,
-// longest first.  All forward loops start together and all reverse loops start
-// together, so at a given step the blocks of the instances still running are a
-// prefix of the block table and a launch covers exactly that prefix.  A block
+// is padded to whole blocks of 256 entries and the blocks of a wave's
+// (instance, shot) pairs are listed in the wave's block table, instances ordered
+// by record length nt, longest first.  Within a wave all forward loops start
+// together and all reverse loops start together, so at a given step the blocks
+// of the pairs still running are a prefix of the table and a launch covers
+// exactly that prefix.  A block
 // belongs to one instance and one shot: it stages the instance's description in
 // shared memory once, and skips its work when the instance is switched off for
 // this call.  The vector bodies are those of the single-instance kernels, so
