@@ -424,3 +424,23 @@ def test_velocity_receivers_match_oracle(vel, comp, opts):
     np.testing.assert_array_equal(g, o["grad"]["g"])
     np.testing.assert_array_equal(fw, o["grad"]["fw"])
     np.testing.assert_array_equal(bk, o["grad"]["bk"])
+
+
+def test_automatic_batches_fit_the_l2():
+    """481x141 (npml 40), 49 shots: the reverse loop's state is about 3.1 MB per
+    shot, so 0.7 of the GB300's L2 holds 28 shots in flight: 6 batches of at
+    most 9 shots on 3 graph branches."""
+    s = survey.config(1)
+    with Engine(**s.engine_args()) as e:
+        q = e.query()
+    import torch
+    l2 = getattr(torch.cuda.get_device_properties(0), "L2_cache_size", None)
+    if not l2:
+        pytest.skip("L2 size not reported")
+    state = (3 * (s.nx + 80) * (s.nz + 80) + 6 * s.nx * s.nz) * 4
+    inflight = int(0.7 * l2 / state)
+    per_branch = max(1, inflight // 3)
+    k = 3 * -(-s.ns // (3 * per_branch))
+    assert q["graph_branches"] == 3 and q["shots_per_batch"] == -(-s.ns // k)
+    if 120e6 < l2 < 135e6:  # GB300
+        assert q["shots_per_batch"] == 9
