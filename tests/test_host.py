@@ -1,6 +1,7 @@
-"""CPU tests of the host-side file contract: SU header layout and values,
-parfile and coord.txt formats."""
+"""CPU tests of the host-side file contract (SU header layout and values,
+parfile and coord.txt formats) and of the Python engine's argument handling."""
 import numpy as np
+import pytest
 
 from swit_gb300 import suio
 
@@ -63,3 +64,25 @@ def test_checkpoint_interval_keeps_boundary_saving_when_it_fits():
     NX, LD, sl = 2121, 736, 9 * 2001 + 6 * 601
     mem = 200 * (-(-6000 // k) * 3 * NX * LD + k * sl) * 4
     assert mem < 200 * 6000 * sl * 4 / 2  # well under boundary saving
+
+
+@pytest.mark.parametrize("kw", [dict(precision="fp16"), dict(path="fast"), dict(adjoint="approx"),
+                                dict(receiver_component="vy"), dict(kernel="tensor")])
+def test_engine_rejects_unknown_options_before_any_gpu_work(kw):
+    from swit_gb300 import Engine, survey
+    s = survey.small()
+    with pytest.raises(ValueError):
+        Engine(**s.engine_args(), **kw)
+
+
+def test_engine_keeps_pinned_float32_host_buffers():
+    """Host float32 inputs reach the C ABI without a copy: a pinned buffer stays
+    pinned, so the engine's host-to-device copy is one DMA."""
+    import torch
+    from swit_gb300.engine import Engine
+    a = torch.arange(12, dtype=torch.float32)
+    assert Engine._f32(a).ctypes.data == a.data_ptr()
+    b = np.arange(12, dtype=np.float32)
+    assert Engine._f32(b).ctypes.data == b.ctypes.data
+    c = Engine._f32(np.arange(12, dtype=np.float64))
+    assert c.dtype == np.float32 and c.flags.c_contiguous
