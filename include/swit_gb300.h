@@ -119,7 +119,8 @@ typedef struct swit_desc {
   int32_t receiver_component; /* 0 = pressure (fd2dmpi); 1 = vx, 2 = vz: the
                                receivers record u or w and the adjoint source
                                enters u or w (dev/solver/fdcore.f90:154-177,
-                               465-485; vec kernels, adjoint_mode 0)          */
+                               465-485; vec kernels; with adjoint_mode 1 the
+                               exact transpose of that recording)           */
 } swit_desc;
 
 /* Creates an engine and allocates its device workspace on the current device.

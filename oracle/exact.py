@@ -44,6 +44,7 @@ class Setup:
         self.dt = float(np.float32(pb.dt))
         self.fs = L + 1
         self.fold = pb.free_surface == 1
+        self.comp = getattr(pb, "comp", 0)  # recorded component: 0 = p, 1 = vx (u), 2 = vz (w)
         self.c = self.pad(np.asarray(vp, np.float32))
         self.den = self.pad(np.asarray(rho, np.float32))
         NX, NZ, dx, dt = self.NX, self.NZ, self.dx, self.dt
@@ -180,10 +181,11 @@ def forward(S, s_idx, src, dc=None, save_d=False):
             w[F - 1, 1:] = w[F, 1:]
             if tl:
                 dw[F - 1, 1:] = dw[F, 1:]
+        rf = (p, u, w)[S.comp]
         for g, (rz, rx) in enumerate(rec):
-            seis[g, it - 1] = p[rz, rx]
+            seis[g, it - 1] = rf[rz, rx]
             if tl:
-                dseis[g, it - 1] = dp[rz, rx]
+                dseis[g, it - 1] = (dp, du, dw)[S.comp][rz, rx]
     return seis, dseis, Ds
 
 
@@ -202,9 +204,10 @@ def adjoint(S, s_idx, adj, Ds):
     Zw, Xw = S.rw()
     F = S.fs
     for it in range(nt, 1, -1):
-        # S6 record
+        # S6 record (p, u or w at the receivers)
+        lr = (lp, lu, lw)[S.comp]
         for g, (rz, rx) in enumerate(rec):
-            lp[rz, rx] += adj[g, it - 1]
+            lr[rz, rx] += adj[g, it - 1]
         # S5 w mirror
         if S.fold:
             lw[F, 1:] += lw[F - 1, 1:]

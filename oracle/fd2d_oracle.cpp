@@ -616,7 +616,7 @@ int gradient_all(const oracle_desc* d, const float* vp, const float* rho, const 
 //   S4  u := (1-ku) u - B Gx(p)         on ix in [2,NX-2], iz in [fs,NZ-1]
 //       w := (1-kw) w - B Gz(p)         on ix in [2,NX-1], iz in [fs,NZ-2]
 //   S5  w(fs-1,:) := w(fs,:)            (free surface)
-//   S6  seis(ig, it) = p(gz, gx)
+//   S6  seis(ig, it) = p(gz, gx)   (u or w for vx / vz receivers)
 // with A = den c^2 dt/dx, B = dt/(den dx).  The adjoint runs it = nt..2 in two
 // gather passes per step (the form the GB300 kernels take, so both evaluate the
 // same expressions in the same order):
@@ -666,12 +666,20 @@ void exact_adjoint_shot(const Setup<R>& S, const oracle_desc& d, int is, const f
     std::vector<R>& mn = m[(it - 1) & 1];
     auto wt = [&](int iz, int ix) -> R { return (fold && iz == F) ? lw(iz, ix) + mo[ix] : lw(iz, ix); };
     const R* D = dsave + (size_t)(it - 1) * NX * NZ;
+    // vx / vz receivers (S6 records u or w): their adjoint sources go into lu or
+    // lw before the step's gathers, in receiver order
+    if (d.comp != 0)
+      for (int ig = 0; ig < ng; ++ig) {
+        F2<R>& lr = d.comp == 1 ? lu : lw;
+        lr(gz[ig], gx[ig]) = lr(gz[ig], gx[ig]) + (R)sadj_in[(size_t)ig * nt + (it - 1)];
+      }
     // K1
     for (int ix = 3; ix <= NX - 2; ++ix)
       for (int iz = F + 1; iz <= NZ - 2; ++iz) {
         R l = (R(1.0) - kp(iz, ix)) * lp(iz, ix);
-        for (int ig = 0; ig < ng; ++ig)
-          if (gz[ig] == iz && gx[ig] == ix) l = l + (R)sadj_in[(size_t)ig * nt + (it - 1)];
+        if (d.comp == 0)
+          for (int ig = 0; ig < ng; ++ig)
+            if (gz[ig] == iz && gx[ig] == ix) l = l + (R)sadj_in[(size_t)ig * nt + (it - 1)];
         l = l - c1 * (B(iz, ix - 1) * lu(iz, ix - 1));
         l = l + c1 * (B(iz, ix) * lu(iz, ix));
         if (ix - 2 >= 2) l = l - c2 * (B(iz, ix - 2) * lu(iz, ix - 2));
@@ -741,7 +749,6 @@ int exact_all(const oracle_desc* d, const float* vp, const float* rho, const flo
               R* gsrc, R* seis_out, int nthreads) {
   int rc = check_desc(d);
   if (rc) return rc;
-  if (d->comp != 0) return -2;  // pressure receivers only
   Setup<R> S;
   S.build(*d, vp, rho);
   const size_t N = (size_t)S.NX * S.NZ, NS = (size_t)d->ngmax * d->nt;

@@ -535,6 +535,9 @@ void launch_exact_steps(swit_engine* e, int shot0, int nb, cudaStream_t st, int 
   const dim3 block = vec_block(e), g0 = vec_grid(e, 0, nb), g1 = vec_grid(e, 1, nb);
   const VecList l0 = vec_list(e, 0), l1 = vec_list(e, 1);
   for (int it = it_hi; it >= it_lo; --it) {
+    if (e->rcomp)
+      launch_pdl(e->pdl, k_xinject_vel<R>, dim3((e->NX + 255) / 256, nb), dim3(256), st, g, make_rec(e), x, it,
+                 shot0);
     launch_pdl(e->pdl, k_xadj_p<R>, g0, block, st, g, l0, make_rec(e), make_src(e), x, it, shot0);
     launch_pdl(e->pdl, k_xadj_uw<R>, g1, block, st, g, l1, x, it, shot0);
   }
@@ -1915,9 +1918,9 @@ int swit_create(const swit_desc* d, swit_engine** out) {
     delete e;
     return fail(SWIT_E_ARG, "receiver_component must be 0 (p), 1 (vx) or 2 (vz) (got %d)", d->receiver_component);
   }
-  if (d->receiver_component && (e->variant != 3 || e->exact)) {
+  if (d->receiver_component && e->variant != 3) {
     delete e;
-    return fail(SWIT_E_ARG, "vx / vz receivers run on the vec kernels with fd2dmpi's adjoint (adjoint_mode 0)");
+    return fail(SWIT_E_ARG, "vx / vz receivers run on the vec kernels (kernel_variant 0 or 3)");
   }
   e->rcomp = d->receiver_component;
   if (e->exact) e->SL = e->NX * e->LD;  // the strip buffer holds D of each step

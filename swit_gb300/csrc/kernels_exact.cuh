@@ -7,7 +7,7 @@
 //   S4  u := (1-ku) u - B Gx(p)          ix in [2, NX-2], iz in [fs, NZ-1]
 //       w := (1-kw) w - B Gz(p)          ix in [2, NX-1], iz in [fs, NZ-2]
 //   S5  w(fs-1, :) := w(fs, :)           (free surface)
-//   S6  seis(ig, it) = p(gz, gx)
+//   S6  seis(ig, it) = p(gz, gx)        (u or w for vx / vz receivers)
 // with A = den c^2 dt/dx and B = dt/(den dx).  Its transpose, run for it = nt
 // .. 2 on the adjoint fields (lp, lu, lw) in the engine's backward buffers, is
 // two gathers per step, each thread owning one 4-row vector as in
@@ -95,8 +95,8 @@ __global__ void __launch_bounds__(256) k_xadj_p(Grid<R> g, VecList L, Receivers 
   R l[4];
 #pragma unroll
   for (int j = 0; j < 4; ++j) l[j] = (R(1.0) - kp.x[j]) * lp.x[j];
-  // adjoint sources of this column, in receiver order
-  if (iz0 + 3 >= rec.zlo[s] && iz0 <= rec.zhi[s]) {
+  // adjoint sources of this column, in receiver order (pressure receivers)
+  if (rec.comp == 0 && iz0 + 3 >= rec.zlo[s] && iz0 <= rec.zhi[s]) {
     const int c0 = rec.colptr[(size_t)s * (NX + 2) + ix], c1 = rec.colptr[(size_t)s * (NX + 2) + ix + 1];
     for (int e = c0; e < c1; ++e) {
       const int j = rec.zrow[e] - iz0;
@@ -183,6 +183,25 @@ __global__ void __launch_bounds__(256, SWIT_VEC_MINB_R(R)) k_xadj_uw(Grid<R> g, 
     lw.x[j] = a;
   }
   st4(x.lw + off, k4, lw);
+}
+
+// vx / vz receivers record u / w (S6), so the transposed record adds the
+// adjoint sources of step it to lu / lw before the step's two gathers; one
+// thread per column and shot, in receiver order.
+template <class R>
+__global__ void k_xinject_vel(Grid<R> g, Receivers rec, XAdj<R> x, int it, int shot0) {
+  const int ix = blockIdx.x * blockDim.x + threadIdx.x + 1;
+  const int s = shot0 + blockIdx.y;
+  pdl_enter();
+  if (ix > g.NX) return;
+  const int* cp = rec.colptr + (size_t)s * (g.NX + 2);
+  const int e1 = cp[ix + 1];
+  if (cp[ix] == e1) return;
+  R* f = (rec.comp == 1 ? x.lu : x.lw) + (size_t)s * g.FSZ + (size_t)(ix - 1) * g.LD;
+  for (int e = cp[ix]; e < e1; ++e) {
+    const int z = rec.zrow[e];
+    f[z - 1] = f[z - 1] + x.adj_t[((size_t)s * g.nt + (it - 1)) * g.ngmax + rec.ig[e]];
+  }
 }
 
 // dJ/dvp on the interior, (nx, nz) z-fastest: per PML point the shots' gA in

@@ -52,7 +52,7 @@ def _desc(s, **over):
     (dict(adjoint_mode=2), _lib.SwitError), (dict(adjoint_mode=1, kernel_variant=1), _lib.SwitError),
     (dict(adjoint_mode=1, kernel_variant=6), _lib.SwitError),
     (dict(receiver_component=3), _lib.SwitError), (dict(receiver_component=1, kernel_variant=1), _lib.SwitError),
-    (dict(receiver_component=2, adjoint_mode=1), _lib.SwitError),
+    (dict(receiver_component=2, kernel_variant=6), _lib.SwitError),
 ])
 def test_create_rejects_bad_descriptions_before_any_gpu_work(over, code):
     lib = _lib.load()

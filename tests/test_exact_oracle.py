@@ -88,3 +88,21 @@ def test_gather_form_with_duplicate_receivers_and_ragged_shots():
     g, gsrc = X.gradient(pb, s.vp_true, rho, src, rr)
     o = O.exact(pb, s.vp_true, rho, src, rr, fp64=True)
     assert rel(o["g"], g) <= 1e-12 and rel(o["gsrc"], gsrc) <= 1e-12
+
+
+@pytest.mark.parametrize("comp", ["vx", "vz"])
+def test_exact_adjoint_of_velocity_receivers(comp):
+    """vx / vz receivers record u / w; the transposed record puts the adjoint
+    source into the adjoint u / w.  Dot products and the gather form as for p."""
+    s, pb0, rho, src, r, rng = case(1)
+    pb = O.Problem(s.nx, s.nz, s.npml, s.nt, s.dx, s.dt, s.src_xz, s.rec_xz, free_surface=1, comp=comp)
+    g, gsrc = X.gradient(pb, s.vp_true, rho, src, r)
+    dvp = rng.standard_normal((s.nx, s.nz))
+    seis, dseis = X.tangent(pb, s.vp_true, rho, src, dvp)
+    np.testing.assert_array_equal(seis, O.forward(pb, s.vp_true, rho, src, store=False, fp64=True)["seis"])
+    a, b = np.sum(dseis * r), np.sum(dvp * g)
+    assert abs(a - b) <= 1e-12 * abs(a)
+    a, b = np.sum(seis * r), np.sum(src.astype(np.float64) * gsrc)
+    assert abs(a - b) <= 1e-12 * abs(a)
+    o = O.exact(pb, s.vp_true, rho, src, r, fp64=True)
+    assert rel(o["g"], g) <= 1e-12 and rel(o["gsrc"], gsrc) <= 1e-12

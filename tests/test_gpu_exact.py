@@ -203,3 +203,18 @@ def test_exact_loop_split_into_several_graphs(base, monkeypatch):
     _, g, gs = run(base, shots_per_batch=1)
     np.testing.assert_array_equal(g, base["ref"]["g"])
     np.testing.assert_array_equal(gs, base["ref"]["gsrc"])
+
+
+@pytest.mark.parametrize("comp", ["vx", "vz"])
+@pytest.mark.parametrize("opts", [dict(), dict(path="plain"), dict(checkpoint_every=40, shots_per_batch=1)])
+def test_exact_adjoint_of_velocity_receivers_matches_oracle(base, comp, opts):
+    s = base["s"]
+    pb = O.Problem(s.nx, s.nz, s.npml, s.nt, s.dx, s.dt, s.src_xz, s.rec_xz, free_surface=s.free_surface, comp=comp)
+    ref = O.exact(pb, s.vp_true, base["rho"], base["src"], base["adj"])
+    with engine(s, receiver_component=comp, **opts) as e:
+        e.set_model(s.vp_true, base["rho"])
+        seis = e.forward(base["src"], save_boundary=True)
+        g, gs = e.backward_exact(base["adj"])
+    np.testing.assert_array_equal(seis, ref["seis"])
+    np.testing.assert_array_equal(g, ref["g"])
+    np.testing.assert_array_equal(gs, ref["gsrc"])
