@@ -20,6 +20,30 @@ def declared_symbols():
     return sorted(set(re.findall(r"\b(swit_[a-z0-9_]+)\s*\(", txt)))
 
 
+def declared_desc_fields():
+    txt = open(HEADER).read()
+    txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+    body = txt[txt.index("typedef struct swit_desc {"):txt.index("} swit_desc;")]
+    out = []
+    for decl in body.split("{", 1)[1].split(";"):
+        if not decl.strip():
+            continue
+        head, *rest = decl.strip().split(",")
+        out.append(re.findall(r"([a-z_][a-z0-9_]*)\s*$", head.strip())[0])
+        out += [r.strip() for r in rest]
+    return out
+
+
+def test_swit_desc_fields_match_the_ctypes_binding_and_the_integration_stub():
+    """The header's struct, the library binding and the documented ctypes stub
+    list the same fields in the same order (a missing field shifts every later one)."""
+    fields = [f[0] for f in _lib.SwitDesc._fields_]
+    assert declared_desc_fields() == fields
+    doc = open(os.path.join(os.path.dirname(HEADER), os.pardir, "INTEGRATION.md")).read()
+    stub = doc[doc.index("class SwitDesc"):doc.index("lib.swit_create")]
+    assert re.findall(r'\("(\w+)", C\.c_', stub) == fields
+
+
 def test_library_builds_and_exports_every_declared_symbol():
     lib = _lib.load()
     names = declared_symbols()
