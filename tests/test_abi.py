@@ -44,6 +44,26 @@ def test_swit_desc_fields_match_the_ctypes_binding_and_the_integration_stub():
     assert re.findall(r'\("(\w+)", C\.c_', stub) == fields
 
 
+def declared_arity():
+    txt = open(HEADER).read()
+    txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+    out = {}
+    for name, args in re.findall(r"\b(swit_[a-z0-9_]+)\s*\(([^)]*)\)\s*;", txt, flags=re.S):
+        args = args.strip()
+        out[name] = 0 if args in ("", "void") else args.count(",") + 1
+    return out
+
+
+def test_binding_argument_counts_match_the_header():
+    lib = _lib.load()
+    arity = declared_arity()
+    assert set(arity) == set(_lib.EXPORTS)
+    for name, n in arity.items():
+        argtypes = getattr(lib, name).argtypes
+        if argtypes is not None:
+            assert len(argtypes) == n, (name, len(argtypes), n)
+
+
 def test_library_builds_and_exports_every_declared_symbol():
     lib = _lib.load()
     names = declared_symbols()
