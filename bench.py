@@ -299,7 +299,8 @@ def run_mine(args):
     rho = sv.rho(sv.vp_true)
     src = sv.source()[lo:hi].copy()
     from swit_gb300.engine import checkpoint_interval
-    ckpt = (checkpoint_interval(sv.nx, sv.nz, sv.npml, sv.nt, per_rank, 0) if args.checkpoint == "auto"
+    ckpt = (checkpoint_interval(sv.nx, sv.nz, sv.npml, sv.nt, per_rank, 0, exact=args.adjoint == "exact")
+            if args.checkpoint == "auto"
             else int(args.checkpoint))
     opts = dict(shots_per_batch=args.batch, block_x=args.block_x, kernel=args.kernel, checkpoint_every=ckpt,
                 graph_branches=args.branches, adjoint=args.adjoint)

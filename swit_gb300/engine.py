@@ -356,17 +356,19 @@ class MultiEngine:
         self.close()
 
 
-def checkpoint_interval(nx, nz, npml, nt, ns, budget_bytes, ng=None, fp64=False):
+def checkpoint_interval(nx, nz, npml, nt, ns, budget_bytes, ng=None, fp64=False, exact=False):
     """Memory strategy for a survey: 0 (boundary saving, fd2dmpi's own) when the
     engine with the strips of all shots fits in ``budget_bytes`` (wavefields,
     imaging sums and trace staging included; ng receivers per shot, default nx),
     else the checkpoint interval k that minimises checkpoints + strip buffer,
     ns * (ceil(nt/k) * 3 * NX * LD + k * (9 nx + 6 nz)) values (the allocation of
-    swit_create with checkpoint_every = k)."""
+    swit_create with checkpoint_every = k).  exact: an exact-adjoint engine,
+    whose per-step record is a whole NX * LD divergence field instead of the
+    strips."""
     esz = 8 if fp64 else 4
     NX, NZ = nx + 2 * npml, nz + 2 * npml
     fsz = NX * ((NZ + 31) // 32) * 32
-    sl = 9 * nx + 6 * nz
+    sl = fsz if exact else 9 * nx + 6 * nz
     ng = nx if ng is None else ng
     rest = 12 * ns * fsz * esz + ns * ng * nt * (3 * esz + 4)  # fields and sums; seis, adjoint, staging, input
     if ns * nt * sl * esz + rest <= budget_bytes:

@@ -66,6 +66,17 @@ def test_checkpoint_interval_keeps_boundary_saving_when_it_fits():
     assert mem < 200 * 6000 * sl * 4 / 2  # well under boundary saving
 
 
+def test_checkpoint_interval_of_the_exact_adjoint():
+    """An exact-adjoint engine stores a whole divergence field per step (98.5 GB at
+    481 x 141, 49 shots, nt 4000): it fits 150 GB, not 50 GB, where the interval
+    that minimises checkpoints + records is about sqrt(3 nt)."""
+    from swit_gb300.engine import checkpoint_interval
+    assert checkpoint_interval(481, 141, 40, 4000, 49, 150e9, exact=True) == 0
+    k = checkpoint_interval(481, 141, 40, 4000, 49, 50e9, exact=True)
+    assert 80 <= k <= 140
+    assert checkpoint_interval(481, 141, 40, 4000, 49, 50e9) == 0  # fd2dmpi's strips: 4 GB
+
+
 @pytest.mark.parametrize("kw", [dict(precision="fp16"), dict(path="fast"), dict(adjoint="approx"),
                                 dict(receiver_component="vy"), dict(kernel="tensor")])
 def test_engine_rejects_unknown_options_before_any_gpu_work(kw):
