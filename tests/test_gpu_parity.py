@@ -444,3 +444,24 @@ def test_automatic_batches_fit_the_l2():
     assert q["graph_branches"] == 3 and q["shots_per_batch"] == -(-s.ns // k)
     if 120e6 < l2 < 135e6:  # GB300
         assert q["shots_per_batch"] == 9
+
+
+@pytest.mark.parametrize("idx,ns,nt", [(0, 5, 2000), (1, 4, 800)])
+def test_benchmark_configurations_match_oracle(idx, ns, nt):
+    """The plain small configuration (201x101, dx 25 m, nt 2000, 5 shots) in full
+    and the Marmousi-like one (481x141, npml 40) with 4 of its shots and 800
+    steps, through the C ABI against the FP32 oracle on the same seeded inputs:
+    seismograms within 1e-5 and gradient and illuminations within 1e-4 relative
+    L2, the engine's specified bounds."""
+    s = survey.config(idx, ns=ns, nt=nt)
+    pb = O.Problem(s.nx, s.nz, s.npml, s.nt, s.dx, s.dt, s.src_xz, s.rec_xz, free_surface=s.free_surface)
+    rho = s.rho(s.vp_true)
+    src = s.source()
+    obs = O.forward(pb, s.vp_true, rho, src, store=False)["seis"]
+    ref = O.gradient(pb, s.vp_init, rho, src, obs, return_seis=True)
+    with Engine(**s.engine_args()) as e:
+        e.set_model(s.vp_init, rho)
+        out = e.gradient_l2(src, obs, return_seis=True)
+    assert rel(out["seis"], ref["seis"]) <= SEIS_TOL
+    for mine, k in ((out["grad"], "g"), (out["illum_fw"], "fw"), (out["illum_bk"], "bk")):
+        assert rel(mine, ref[k]) <= GRAD_TOL, k
