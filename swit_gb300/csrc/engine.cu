@@ -811,7 +811,8 @@ int forward_impl(swit_engine* e, const float* src, void* seis, bool store, int o
 }
 
 // Reverse loop of the exact adjoint over all shots: plain path one shot at a
-// time, batched path captured once into a graph (batches on concurrent branches).
+// time, batched path captured once into bounded graphs (batches on concurrent
+// branches), or issued straight into a caller's capture.
 template <class R>
 int run_exact_loop(swit_engine* e, cudaStream_t st) {
   if (e->path == 1) {
