@@ -106,3 +106,53 @@ def test_exact_adjoint_of_velocity_receivers(comp):
     assert abs(a - b) <= 1e-12 * abs(a)
     o = O.exact(pb, s.vp_true, rho, src, r, fp64=True)
     assert rel(o["g"], g) <= 1e-12 and rel(o["gsrc"], gsrc) <= 1e-12
+
+
+def test_exact_adjoint_properties_on_random_small_problems():
+    """Random small grids, PML widths, record lengths, free-surface flags,
+    receiver components and geometries (receivers on the surface row, two on one
+    node, ragged counts): the numpy forward equals the C++ oracle's in FP64, the
+    dot-product identities hold and the gather form equals the literal transpose."""
+    hyp = pytest.importorskip("hypothesis")
+    st = pytest.importorskip("hypothesis.strategies")
+
+    @hyp.settings(max_examples=25, deadline=None, derandomize=True)
+    @hyp.given(nx=st.integers(10, 22), nz=st.integers(10, 16), npml=st.integers(2, 6), nt=st.integers(20, 60),
+               fs=st.sampled_from([0, 1]), comp=st.sampled_from(["p", "vx", "vz"]), ns=st.integers(1, 3),
+               seed=st.integers(0, 10_000))
+    def check(nx, nz, npml, nt, fs, comp, ns, seed):
+        rng = np.random.default_rng(seed)
+        dx = 10.0
+        vp = rng.uniform(1500.0, 3000.0, (nx, nz)).astype(np.float32)
+        rho = (310 * vp.astype(np.float64) ** 0.25).astype(np.float32)
+        ngmax = int(rng.integers(1, 6))
+        xs = rng.uniform(0, (nx - 1) * dx, ns)
+        zs = rng.choice([0.0, dx, 2 * dx, 3 * dx], ns)
+        rec = np.stack([rng.uniform(0, (nx - 1) * dx, (ns, ngmax)), rng.choice([0.0, dx, 2 * dx], (ns, ngmax))], -1)
+        if ngmax > 1:
+            rec[:, 1] = rec[:, 0]  # two receivers on one node
+        ng = rng.integers(1, ngmax + 1, ns).astype(np.int32)
+        pb = O.Problem(nx, nz, npml, nt, dx, 0.001, np.stack([xs, zs], 1), rec.astype(np.float32), free_surface=fs,
+                       ng=ng, comp=comp)
+        t = np.arange(nt)
+        src = np.stack([np.sin(0.3 * (k + 1) * t) * np.exp(-((t - 10) / 5.0) ** 2) for k in range(ns)])
+        src = src.astype(np.float32)
+        r = rng.standard_normal((ns, ngmax, nt)).astype(np.float32)
+        for i in range(ns):
+            r[i, ng[i]:] = 0.0  # traces beyond a shot's receiver count carry nothing
+        S = X.Setup(pb, vp, rho)
+        ref = O.forward(pb, vp, rho, src, store=False, fp64=True)["seis"]
+        for i in range(ns):
+            np.testing.assert_array_equal(X.forward(S, i, src[i])[0], ref[i, :ng[i]])
+        g, gsrc = X.gradient(pb, vp, rho, src, r)
+        dvp = rng.standard_normal((nx, nz))
+        seis, dseis = X.tangent(pb, vp, rho, src, dvp)
+        a, b = np.sum(dseis * r), np.sum(dvp * g)
+        assert abs(a - b) <= 1e-11 * max(abs(a), 1e-300)
+        a, b = np.sum(seis * r), np.sum(src.astype(np.float64) * gsrc)
+        assert abs(a - b) <= 1e-11 * max(abs(a), 1e-300)
+        o = O.exact(pb, vp, rho, src, r, fp64=True)
+        assert np.linalg.norm(o["g"] - g) <= 1e-12 * max(np.linalg.norm(g), 1e-300)
+        assert np.linalg.norm(o["gsrc"] - gsrc) <= 1e-12 * max(np.linalg.norm(gsrc), 1e-300)
+
+    check()
