@@ -96,6 +96,14 @@ class Job:
         self.free_surface = int(read_par(parfile, "FREESURFACE", "1"))
         self.npml = int(read_par(parfile, "NPML", "40"))
         self.store_snap = int(read_par(parfile, "STORE_SNAP", "0"))
+        # the dev solver's recorded component (dev/solver/io.f90:77, fdcore.f90:155-177): p, vx or vz
+        comp = read_par(parfile, "DATA_COMP", "p")
+        if comp[:1] == "p":
+            self.data_comp = "p"
+        elif comp[:2] in ("vx", "vz"):
+            self.data_comp = comp[:2]
+        else:
+            raise ValueError("data comp not recognized: %s" % comp)
         self.dx = np.float32(float(read_par(parfile, "DX", "-1.0")))
         self.dt = np.float32(float(read_par(parfile, "DT_WORK", "-1.0")))
         if self.nx <= 0 or self.nz <= 0 or self.nt <= 0 or self.dx <= 0 or self.dt <= 0:
@@ -108,7 +116,7 @@ class Job:
 def _engine(job, src_xz, rec_xz, ng):
     from .engine import Engine
     return Engine(job.nx, job.nz, job.npml, job.nt, float(job.dx), float(job.dt), src_xz, rec_xz,
-                  free_surface=job.free_surface, ng=ng)
+                  free_surface=job.free_surface, ng=ng, receiver_component=job.data_comp)
 
 
 def _model(job):

@@ -21,6 +21,23 @@ def test_parfile_prefix_semantics(tmp_path):
     assert fd2dmpi.read_par(str(p), "NPML", "40") == "40"   # only the first 1000 lines
 
 
+@pytest.mark.parametrize("line,comp", [("", "p"), ("DATA_COMP=p\n", "p"), ("DATA_COMP=vx\n", "vx"),
+                                       ("DATA_COMP=vz\n", "vz"), ("DATA_COMP=pressure\n", "p")])
+def test_data_comp_key_of_the_dev_solver(tmp_path, line, comp):
+    """DATA_COMP (dev/solver/io.f90:77, default p) picks the recorded component by
+    its first letters as dev/solver/fdcore.f90:155-177 does."""
+    p = tmp_path / "par"
+    p.write_text("NX=20\nNZ=10\nNT_WORK=50\nDX=10.0\nDT_WORK=0.001\n" + line)
+    assert fd2dmpi.Job(str(p)).data_comp == comp
+
+
+def test_unknown_data_comp_is_an_error(tmp_path):
+    p = tmp_path / "par"
+    p.write_text("NX=20\nNZ=10\nNT_WORK=50\nDX=10.0\nDT_WORK=0.001\nDATA_COMP=vy\n")
+    with pytest.raises(ValueError):
+        fd2dmpi.Job(str(p))
+
+
 def test_coord_grouping(tmp_path):
     p = tmp_path / "coord.txt"
     src = np.array([[0.0, 25.0], [100.0, 25.0]])
