@@ -13,6 +13,8 @@ and writes the same outputs:
                                                                     (solver.f90:263-279)
 
 so toolbox/solver.py runs unchanged with this program in place of fd2dmpi.
+The dev solver's DATA_COMP key (p, vx or vz; dev/solver/io.f90:77) selects the
+recorded component.
 The adjoint job reads the saved strips and end states when they exist and
 otherwise recomputes them on the GPU.  Under mpirun every rank but rank 0
 exits at once: all shots run batched on one GPU.  The exit status is 0 on
