@@ -64,6 +64,44 @@ def test_binding_argument_counts_match_the_header():
             assert len(argtypes) == n, (name, len(argtypes), n)
 
 
+def test_plain_c_client_compiles_links_and_gets_argument_errors(tmp_path):
+    """tests/c_abi_client.c uses only include/swit_gb300.h: it compiles as C99,
+    links against the engine library and, given a bad description, gets
+    SWIT_E_ARG and a message without touching a GPU."""
+    import shutil
+    import subprocess
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if not cc:
+        pytest.skip("no C compiler")
+    libdir = os.path.dirname(_lib.load()._name)
+    exe = str(tmp_path / "c_abi_client")
+    src = os.path.join(os.path.dirname(os.path.abspath(__file__)), "c_abi_client.c")
+    subprocess.run([cc, "-std=c99", "-O2", "-Wall", "-Werror", "-I", os.path.dirname(HEADER), src, "-o", exe,
+                    "-L", libdir, "-lswit_gb300", "-Wl,-rpath," + libdir, "-lm"], check=True)
+    out = subprocess.run([exe, "invalid"], capture_output=True, text=True)
+    assert out.returncode == 0, out.stdout + out.stderr
+    assert "nx and nz must be >= 8" in out.stdout
+
+
+@pytest.mark.gpu
+def test_plain_c_client_runs_a_gradient(tmp_path):
+    """The same C client, without arguments: create, set model, forward, and a
+    Waveform-misfit gradient with host buffers, all through the C ABI."""
+    import shutil
+    import subprocess
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if not cc:
+        pytest.skip("no C compiler")
+    libdir = os.path.dirname(_lib.load()._name)
+    exe = str(tmp_path / "c_abi_client")
+    src = os.path.join(os.path.dirname(os.path.abspath(__file__)), "c_abi_client.c")
+    subprocess.run([cc, "-std=c99", "-O2", "-I", os.path.dirname(HEADER), src, "-o", exe, "-L", libdir,
+                    "-lswit_gb300", "-Wl,-rpath," + libdir, "-lm"], check=True)
+    out = subprocess.run([exe], capture_output=True, text=True, timeout=300)
+    assert out.returncode == 0, out.stdout + out.stderr
+    assert out.stdout.startswith("misfit ")
+
+
 def test_library_builds_and_exports_every_declared_symbol():
     lib = _lib.load()
     names = declared_symbols()
