@@ -20,6 +20,7 @@ FUSED = False  # the fused kernels are slower on GB300 at every measured shape
 
 
 def candidates(ns, nz_pml):
+    """Launch configurations to time for ns shots (nz_pml: padded rows, for the fused kernels' limit)."""
     out = []
     batches = sorted({ns, max(1, (ns + 1) // 2), max(1, (ns + 3) // 4)}, reverse=True)
     if FUSED and nz_pml <= 1024:

@@ -134,6 +134,7 @@ def _sources(job, ns, folder):
 
 
 def forward_modeling(job):
+    """jobtype=forward_modeling (fd2dmpi/solver.f90:36-116): seismograms, and strips with STORE_SNAP=1."""
     src_xz, rec_xz, ng = read_coord(job.coordfile)
     ns = src_xz.shape[0]
     vp, rho = _model(job)
@@ -158,6 +159,7 @@ def forward_modeling(job):
 
 
 def adjoint_modeling(job):
+    """jobtype=adjoint_modeling (fd2dmpi/solver.f90:120-289): vp kernel and illuminations."""
     src_xz, rec_xz, ng = read_coord(job.coordfile)
     ns, ngmax = src_xz.shape[0], rec_xz.shape[1]
     vp, rho = _model(job)
@@ -188,6 +190,7 @@ def adjoint_modeling(job):
 
 
 def main(argv=None):
+    """fd2dmpi par=<parfile> (fd2dmpi/fd2dmpi.f90:16-34); returns the exit status."""
     argv = sys.argv[1:] if argv is None else argv
     parfile = "fdparfile"  # fd2dmpi.f90:22 default of readCmd('par', ...)
     for a in argv:

@@ -137,18 +137,22 @@ class _GlobalCorrelation(torch.autograd.Function):
 
 
 def waveform(syn, obs, dt):
+    """L2 waveform misfit; gradient = syn - obs (misfit.py:128-148, 263-282)."""
     return _Waveform.apply(syn, obs, float(dt))
 
 
 def envelope(syn, obs, dt):
+    """Envelope misfit with its adjoint source (misfit.py:151-184, 285-309)."""
     return _Envelope.apply(syn, obs, float(dt))
 
 
 def traveltime(syn, obs, dt):
+    """Cross-correlation traveltime misfit (misfit.py:188-215, 312-334, 359-373)."""
     return _Traveltime.apply(syn, obs, float(dt))
 
 
 def global_correlation(syn, obs, dt):
+    """Normalised global-correlation misfit (misfit.py:219-242, 338-355)."""
     return _GlobalCorrelation.apply(syn, obs, float(dt))
 
 

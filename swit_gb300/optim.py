@@ -18,14 +18,17 @@ import torch
 
 
 def pollak_ribere(g_now, g_old):
+    """Polak-Ribiere beta (inversion.py:485-492)."""
     return torch.dot(g_now, g_now - g_old) / torch.dot(g_old, g_old)
 
 
 def check_descent(d_now, g_now):
+    """<d, g> / <g, g>: positive when d is not a descent direction (inversion.py:501-505)."""
     return torch.dot(d_now, g_now) / torch.dot(g_now, g_now)
 
 
 def model_update(vp, update, vpmax, vpmin):
+    """vp + update clipped to [vpmin, vpmax] (inversion.py:474-482)."""
     return torch.clamp(vp + update, min=vpmin, max=vpmax)
 
 
@@ -46,6 +49,7 @@ def init_state(scheme, n, device="cuda", memory=5):
 
 
 def nlcg_direction(st, cg_itmax=6):
+    """NLCG search direction with restarts (inversion.py:111-171)."""
     g_now, g_old, d_old = st["g_now"], st["g_old"], st["d_old"]
     st["cg_it"] += 1
     if st["cg_it"] == 1:
@@ -71,6 +75,7 @@ def nlcg_direction(st, cg_itmax=6):
 
 
 def lbfgs_direction(st):
+    """L-BFGS two-loop direction with memory 5 and restarts (inversion.py:174-271)."""
     g_now, g_old, v_now, v_old = st["g_now"], st["g_old"], st["v_now"], st["v_old"]
     S, Y = st["S"], st["Y"]
     st["lbfgs_it"] += 1

@@ -29,6 +29,7 @@ def integrated_source(wavelet):
 
 
 def gardner(vp):
+    """Gardner density 310 vp^0.25 (examples/case-01-marmousi2/SWIT_workflow_LBGFS.py:49-50)."""
     return (np.power(np.asarray(vp, np.float64), 0.25) * 310).astype(np.float32)
 
 
