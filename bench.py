@@ -179,17 +179,54 @@ class ClockSampler:
 
 
 # --------------------------------------------------------------------- arms
-def cpu_baseline(sv, rho, src, obs, threads, kind="port"):
-    """Oracle (C++ restatement of fd2dmpi, FP32, -O3, one shot per thread with
-    fd2dmpi's static shot split) on min(ns, threads) shots at full nt."""
+def rel_l2(a, b):
+    """||a - b|| / ||b|| in float64 (0 when b is all zero and a equals it)."""
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    nb = float(np.linalg.norm(b))
+    return float(np.linalg.norm(a - b) / nb) if nb > 0 else float(np.linalg.norm(a))
+
+
+def _np(x):
+    return x.detach().cpu().numpy() if hasattr(x, "detach") else np.asarray(x)
+
+
+def oracle_gradient(sv, rho, src, obs, threads):
+    """All shots' Waveform gradient on the CPU oracle (FP32, one shot per thread,
+    fd2dmpi's static split); returns (result, wall seconds)."""
     from oracle import oracle as O
-    n = min(sv.ns, threads)
-    pb = O.Problem(sv.nx, sv.nz, sv.npml, sv.nt, sv.dx, sv.dt, sv.src_xz[:n], sv.rec_xz[:n])
+    pb = O.Problem(sv.nx, sv.nz, sv.npml, sv.nt, sv.dx, sv.dt, sv.src_xz, sv.rec_xz)
     t0 = time.perf_counter()
-    O.gradient(pb, sv.vp_init, rho, src[:n], obs[:n], nthreads=threads)
-    wall = time.perf_counter() - t0
-    return {"value": n / wall, "unit": UNIT, "cores": threads, "kind": kind,
-            "sample": "%d of %d shots at full nt=%d, one shot per thread, %.1f s wall" % (n, sv.ns, sv.nt, wall)}
+    ref = O.gradient(pb, sv.vp_init, rho, src, obs, return_seis=True, nthreads=threads)
+    return ref, time.perf_counter() - t0
+
+
+def full_size_parity(sv, rho, src_d, obs_d, mine, ref32=None):
+    """Error of the timed FP32 result at the benchmark's own size: against the
+    FP64 build of the same kernels (the error FP32 arithmetic adds) and, when
+    given, against the FP32 oracle (bit-for-bit agreement expected: the same
+    statements in the same order, no FMA)."""
+    from swit_gb300 import Engine
+    e64 = Engine(sv.nx, sv.nz, sv.npml, sv.nt, sv.dx, sv.dt, sv.src_xz, sv.rec_xz, free_surface=sv.free_surface,
+                 precision="fp64")
+    e64.set_model(sv.vp_init, rho)
+    r64 = e64.gradient_l2(src_d, obs_d, return_seis=True)
+    e64.close()
+    m = {k: _np(mine[k]) for k in ("seis", "grad", "illum_fw", "illum_bk")}
+    out = {"shots": int(sv.ns), "nt": int(sv.nt),
+           "vs_fp64_build": {k + "_rel_l2": rel_l2(m[k], _np(r64[k])) for k in m},
+           "tolerance": {"seis_rel_l2": 1e-5, "grad_rel_l2": 1e-4}}
+    if ref32 is not None:
+        names = {"seis": "seis", "grad": "g", "illum_fw": "fw", "illum_bk": "bk"}
+        o = {}
+        for k, rk in names.items():
+            o[k + "_rel_l2"] = rel_l2(m[k], ref32[rk])
+            o[k + "_bit_exact"] = bool(np.array_equal(m[k], ref32[rk]))
+        out["vs_fp32_oracle"] = o
+        out["oracle_vs_fp64_build"] = {k + "_rel_l2": rel_l2(ref32[rk], _np(r64[k])) for k, rk in names.items()}
+    v = out["vs_fp64_build"]
+    out["within_tolerance"] = bool(v["seis_rel_l2"] <= 1e-5 and v["grad_rel_l2"] <= 1e-4)
+    return out
 
 
 def cpu_with_strip_io(sv, rho, src, obs, threads):
@@ -237,7 +274,19 @@ def cpu_with_strip_io(sv, rho, src, obs, threads):
                       "files (%.2f GB), %.1f s wall" % (n, sv.ns, sv.nt, nbytes / 1e9, wall)}
 
 
+def workload_config(sv, shots):
+    """The workload as both arms name it (identical keys and values)."""
+    return {"workload": sv.name, "grid": [sv.nx, sv.nz], "npml": sv.npml, "nt": sv.nt, "shots_per_gpu": shots,
+            "receivers": sv.ng, "dx_m": sv.dx, "dt_s": sv.dt,
+            "l2": "inputs larger than L2: each step streams %.2f GB of boundary strips and %.2f GB of traces"
+                  % (shots * sv.nt * (9 * sv.nx + 6 * sv.nz) * 4 / 1e9, 2 * shots * sv.ng * sv.nt * 4 / 1e9)}
+
+
 def run_reference(args):
+    """The reference arm: the CPU restatement of fd2dmpi (FP32, g++ -O3) on the
+    host cores, one shot per thread with fd2dmpi's static shot split, every
+    step the full workload (all shots, full nt) -- the same work as one step of
+    the GPU arm.  Rank 0 alone runs under torchrun."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
@@ -247,28 +296,30 @@ def run_reference(args):
     threads = os.cpu_count() or 1
     rho = sv.rho(sv.vp_true)
     src = sv.source()
-    n = min(sv.ns, threads)
-    pb = O.Problem(sv.nx, sv.nz, sv.npml, sv.nt, sv.dx, sv.dt, sv.src_xz[:n], sv.rec_xz[:n])
-    obs = O.forward(pb, sv.vp_true, rho, src[:n], store=False, nthreads=threads)["seis"]
-    vals = []
+    pb = O.Problem(sv.nx, sv.nz, sv.npml, sv.nt, sv.dx, sv.dt, sv.src_xz, sv.rec_xz)
+    obs = O.forward(pb, sv.vp_true, rho, src, store=False, nthreads=threads)["seis"]
+    walls = []
     for i in range(args.warmup + args.steps):
-        b = cpu_baseline(sv, rho, src, obs, threads, kind="port")
+        t0 = time.perf_counter()
+        O.gradient(pb, sv.vp_init, rho, src, obs, nthreads=threads)
         if i >= args.warmup:
-            vals.append(b["value"])
-    v = float(np.mean(vals))
+            walls.append(time.perf_counter() - t0)
+    ms_per_step = 1000.0 * float(np.mean(walls))
+    v = sv.ns / (ms_per_step / 1000.0)
     U, B = work_units(sv.nx, sv.nz, sv.npml, sv.nt, sv.ng)
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * n / v,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": sv.name, "grid": [sv.nx, sv.nz], "npml": sv.npml, "nt": sv.nt, "shots": sv.ns,
-                       "receivers": sv.ng, "dx_m": sv.dx, "dt_s": sv.dt, "engine": "CPU restatement of fd2dmpi "
-                       "(oracle/fd2d_oracle.cpp, FP32, g++ -O3); fd2dmpi itself needs gfortran + MPI, absent"},
+            "config": workload_config(sv, sv.ns),
+            "engine": {"path": "CPU restatement of fd2dmpi (oracle/fd2d_oracle.cpp, FP32, g++ -O3), one shot per "
+                               "thread; fd2dmpi itself needs gfortran + MPI, absent"},
             "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
-                             "sample": "%d of %d shots per step at full nt, one shot per thread" % (n, sv.ns)},
+                             "sample": "all %d shots per step at full nt=%d, one shot per thread" % (sv.ns, sv.nt)},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
             "gpts_per_s": v * U / 1e9}
-    # fd2dmpi keeps the strips on disk between its forward and adjoint jobs: one timing with that round trip
-    line["cpu_baseline_with_strip_io"] = cpu_with_strip_io(sv, rho, src, obs, threads)
+    if not args.no_extras:
+        # fd2dmpi keeps the strips on disk between its forward and adjoint jobs: one timing with that round trip
+        line["cpu_baseline_with_strip_io"] = cpu_with_strip_io(sv, rho, src, obs, threads)
     print(json.dumps(line), flush=True)
 
 
@@ -392,13 +443,10 @@ def run_mine(args):
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": sv.name, "grid": [sv.nx, sv.nz], "npml": sv.npml, "nt": sv.nt,
-                       "shots_per_gpu": per_rank, "receivers": sv.ng, "dx_m": sv.dx, "dt_s": sv.dt,
-                       "path": "batched, CUDA graph", "kernel": q["kernel"], "shots_per_launch": q["shots_per_batch"],
-                       "block_x": q["block_x"], "graph_branches": q["graph_branches"], "adjoint": args.adjoint, "parallelism": "shots" + ("" if world == 1 else " x%d ranks" % world),
-                       "l2": "inputs larger than L2: each step streams %.2f GB of boundary strips and %.2f GB of "
-                             "traces" % (per_rank * sv.nt * (9 * sv.nx + 6 * sv.nz) * 4 / 1e9,
-                                         2 * per_rank * sv.ng * sv.nt * 4 / 1e9)},
+            "config": workload_config(sv, per_rank),
+            "engine": {"path": "batched, CUDA graph", "kernel": q["kernel"], "shots_per_launch": q["shots_per_batch"],
+                       "block_x": q["block_x"], "graph_branches": q["graph_branches"], "adjoint": args.adjoint,
+                       "parallelism": "shots" + ("" if world == 1 else " x%d ranks" % world)},
             "autotune": {"trial_steps": 48, "candidates": tuned} if tuned else None,
             "gpts_per_s": value * U / 1e9,
             "hbm_roof_frac_step": (value / world) * B / 1e9 / peak,
@@ -409,7 +457,7 @@ def run_mine(args):
             "gpu_launches": int(args.steps * (q["kernels_per_forward"] + q["kernels_per_backward"] + 5))}
     import hashlib
     gh = last["grad"].detach().float().cpu().numpy()
-    line["config"]["memory"] = {
+    line["engine"]["memory"] = {
         "strategy": "checkpoints every %d steps" % ckpt if ckpt else "boundary saving",
         "device_bytes": q["device_bytes"],
         "gradient_sha256": hashlib.sha256(gh.tobytes()).hexdigest()[:16],
@@ -453,7 +501,15 @@ def run_mine(args):
         line["plain"] = {"value": plain, "unit": UNIT, "sample": "%d shots, one shot per launch, no graph" % nplain}
         line["batched_over_plain"] = (value / world) / plain
         if rank == 0 and world == 1:
-            line["cpu_baseline"] = cpu_baseline(sv, rho, src, obs_d.cpu().numpy(), os.cpu_count() or 1)
+            # every shot of the workload on the oracle: the timed CPU baseline and the FP32 parity target
+            threads = os.cpu_count() or 1
+            ref32, wall = oracle_gradient(sv, rho, src, obs_d.cpu().numpy(), threads)
+            line["cpu_baseline"] = {"value": sv.ns / wall, "unit": UNIT, "cores": threads, "kind": "port",
+                                    "sample": "all %d shots at full nt=%d, one shot per thread, %.1f s wall"
+                                              % (sv.ns, sv.nt, wall)}
+            fin = eng.gradient_l2(src_d, obs_d, return_seis=True)
+            line["parity"] = full_size_parity(sv, rho, src_d, obs_d, fin, ref32)
+            del ref32, fin
     eng.close()
     if rank == 0:
         print(json.dumps(line), flush=True)

@@ -209,12 +209,16 @@ int swit_profile_kernels(swit_engine* e, int32_t launches[4], double mean_ms[4],
  * loads this library holds it until the process exits); larger problems are
  * rejected with SWIT_E_LIMIT before any GPU work.  vp, rho (nx, nz), src (nt)
  * and seis (ng, nt) are DEVICE arrays; rec_x, rec_z (ng) are host arrays.
- * Results equal swit_forward's for the same shot.  The first call on a device
- * looks up the array's device address (cudaGetSymbolAddress) -- make it before
- * any stream capture.  The wavefields are cleared on every call; all calls on a
- * device share the array, so calls that overlap on the GPU race.  The call is
- * ordered on `stream` and returns once the launches are queued; dt is not
- * checked against the CFL limit (the model stays on the device). */
+ * Results equal swit_forward's for the same shot, bit for bit.  The first
+ * call on a device looks up the array's device address (cudaGetSymbolAddress)
+ * -- make it before any stream capture.  The wavefields are cleared on every
+ * call; all calls on a device share the array, so calls that overlap on the GPU
+ * race.  The call is ordered on `stream` and returns once the launches are
+ * queued: receiver and source indices reach the device as kernel arguments, and
+ * the call never waits on the stream.  Because the model stays on the device,
+ * the call cannot report a bad one: a vp or rho value that is not finite and
+ * positive makes the whole seismogram NaN (swit_forward returns SWIT_E_MODEL
+ * instead), and dt is not checked against the CFL limit. */
 int swit_forward_shot_static(int32_t nx, int32_t nz, int32_t npml, int32_t nt, float dx, float dt,
                              int32_t free_surface, float src_x, float src_z, int32_t ng, const float* rec_x,
                              const float* rec_z, const float* vp, const float* rho, const float* src, float* seis,

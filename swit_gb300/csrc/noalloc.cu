@@ -16,7 +16,9 @@
 // call before any stream capture.  All calls on a device share the array, which
 // keeps the last call's contents: the wavefields are cleared at the start of
 // every call, and calls that overlap on the GPU (different streams, or host
-// threads) race on it.
+// threads) race on it.  No call waits on its stream: the receiver and source
+// indices travel as kernel arguments, and the model check runs on the device
+// (a model that fails it gives an all-NaN seismogram).
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -54,7 +56,8 @@ constexpr size_t kOffZr = kOffIg + kMaxReceivers;             // recording row p
 constexpr size_t kOffGx = kOffZr + kMaxReceivers;             // receiver columns (set-up input)
 constexpr size_t kOffGz = kOffGx + kMaxReceivers;             // receiver rows (set-up input)
 constexpr size_t kOffSrc = kOffGz + kMaxReceivers;            // isx, isz, 0, 0
-constexpr size_t kWords = kOffSrc + 4;
+constexpr size_t kOffBad = kOffSrc + 4;                       // 1 if vp or rho is not finite and positive
+constexpr size_t kWords = kOffBad + 4;
 
 static __device__ __align__(256) float g_scratch[kWords];
 
@@ -118,14 +121,22 @@ __global__ void k_static_model(const float* __restrict__ vp, const float* __rest
 // solver.f90:73: interior rows 2..nz), the damping table (pml.f90:80-87) and
 // the receiver table: receivers grouped by column in receiver order, the same
 // table the batched engine builds on the host.
-__global__ void k_static_tables(const float* __restrict__ vp, float* S, int nx, int nz, int L, int NX, int ng,
-                                float dx, float l1000) {
+__global__ void k_static_tables(const float* __restrict__ vp, const float* __restrict__ rho, float* S, int nx,
+                                int nz, int L, int NX, int ng, float dx, float l1000, int isx, int isz) {
   __shared__ float red[1024];
+  __shared__ int bad;
+  if (threadIdx.x == 0) bad = 0;
+  __syncthreads();
   float m = 10000000000.0f;
+  int mine = 0;
   for (int t = threadIdx.x; t < nx * nz; t += blockDim.x) {
+    const float v = vp[t], d = rho[t];
+    // finite and positive, as the engine's model set-up requires (NaN fails both)
+    if (!(v > 0.f && v <= 3.402823466e38f) || !(d > 0.f && d <= 3.402823466e38f)) mine = 1;
     const int jz = t % nz + 1;
-    if (jz > 1) m = fminf(m, vp[t]);
+    if (jz > 1) m = fminf(m, v);
   }
+  if (mine) bad = 1;  // benign race: every writer stores 1
   red[threadIdx.x] = m;
   __syncthreads();
   for (int h = blockDim.x / 2; h > 0; h >>= 1) {
@@ -133,6 +144,11 @@ __global__ void k_static_tables(const float* __restrict__ vp, float* S, int nx, 
     __syncthreads();
   }
   if (threadIdx.x != 0) return;
+  reinterpret_cast<int*>(S + kOffSrc)[0] = isx;
+  reinterpret_cast<int*>(S + kOffSrc)[1] = isz;
+  reinterpret_cast<int*>(S + kOffSrc)[2] = 0;
+  reinterpret_cast<int*>(S + kOffSrc)[3] = 0;
+  reinterpret_cast<int*>(S + kOffBad)[0] = bad;
   const float vmin = red[0];
   const float a = (float)(L - 1) * dx;
   const float kappa = 3.0f * vmin * l1000 / (2.0f * a);
@@ -190,6 +206,28 @@ __global__ void __launch_bounds__(256) k_static_uw(Grid<float> g, Receivers rec,
     if (rec.zrow[e] == iz) seis[(size_t)rec.ig[e] * g.nt + (it - 1)] = P[k];
 }
 
+// Receiver grid indices of receivers [r0, r0 + n), n <= kChunk, passed by value
+// so that the call stages nothing through host memory.
+constexpr int kChunk = 256;
+struct IndexChunk {
+  int gx[kChunk];
+  int gz[kChunk];
+};
+__global__ void k_static_put_indices(float* S, int r0, int n, IndexChunk c) {
+  const int r = threadIdx.x;
+  if (r >= n) return;
+  reinterpret_cast<int*>(S + kOffGx)[r0 + r] = c.gx[r];
+  reinterpret_cast<int*>(S + kOffGz)[r0 + r] = c.gz[r];
+}
+
+// A model that failed the finite-and-positive check gives an all-NaN
+// seismogram: the check runs on the device, so the call itself cannot report it.
+__global__ void k_static_poison(const float* S, float* seis, size_t n) {
+  if (reinterpret_cast<const int*>(S + kOffBad)[0] == 0) return;
+  for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x)
+    seis[t] = __int_as_float(0x7fc00000);
+}
+
 __global__ void k_static_zero_first(float* seis, int ng, int nt) {
   for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < ng; r += gridDim.x * blockDim.x) seis[(size_t)r * nt] = 0.f;
 }
@@ -224,30 +262,24 @@ extern "C" int swit_forward_shot_static(int32_t nx, int32_t nz, int32_t npml, in
   if (rc) return rc;
   cudaStream_t st = (cudaStream_t)stream;
   const int fs = npml + 1;
-  // receiver and source grid indices into the scratch (small host copies from
-  // the stack in chunks, no allocation)
-  int buf[2][256];
-  for (int r0 = 0; r0 < ng; r0 += 256) {
-    const int n = ng - r0 < 256 ? ng - r0 : 256;
+  // receiver and source grid indices: computed here, handed to the device as
+  // kernel arguments (no host staging buffer, no wait on the stream)
+  for (int r0 = 0; r0 < ng; r0 += kChunk) {
+    const int n = ng - r0 < kChunk ? ng - r0 : kChunk;
+    IndexChunk c;
     for (int r = 0; r < n; ++r) {
-      buf[0][r] = npml + (int)(rec_x[r0 + r] / dx) + 1;
-      int igz = npml + (int)(rec_z[r0 + r] / dx) + 1;
-      buf[1][r] = igz == fs ? igz + 1 : igz;
+      c.gx[r] = npml + (int)(rec_x[r0 + r] / dx) + 1;
+      const int igz = npml + (int)(rec_z[r0 + r] / dx) + 1;
+      c.gz[r] = igz == fs ? igz + 1 : igz;
     }
-    cudaError_t ce = cudaMemcpyAsync(S + kOffGx + r0, buf[0], n * sizeof(int), cudaMemcpyHostToDevice, st);
-    if (ce == cudaSuccess)
-      ce = cudaMemcpyAsync(S + kOffGz + r0, buf[1], n * sizeof(int), cudaMemcpyHostToDevice, st);
-    if (ce == cudaSuccess) ce = cudaStreamSynchronize(st);  // buf is reused
-    if (ce != cudaSuccess) return fail(SWIT_E_CUDA, "receiver table: %s", cudaGetErrorString(ce));
+    k_static_put_indices<<<1, kChunk, 0, st>>>(S, r0, n, c);
   }
-  int sidx[4] = {npml + (int)(src_x / dx) + 1, npml + (int)(src_z / dx) + 1, 0, 0};
-  if (sidx[1] == fs) sidx[1] += 1;
-  cudaError_t ce = cudaMemcpyAsync(S + kOffSrc, sidx, sizeof sidx, cudaMemcpyHostToDevice, st);
-  if (ce == cudaSuccess) ce = cudaStreamSynchronize(st);
-  if (ce != cudaSuccess) return fail(SWIT_E_CUDA, "source index: %s", cudaGetErrorString(ce));
+  const int isx = npml + (int)(src_x / dx) + 1;
+  int isz = npml + (int)(src_z / dx) + 1;
+  if (isz == fs) isz += 1;
 
   k_static_model<<<152 * 4, 256, 0, st>>>(vp, rho, S, nx, nz, npml, NX, NZ, LD, dt, dx);
-  k_static_tables<<<1, 1024, 0, st>>>(vp, S, nx, nz, npml, NX, ng, dx, (float)std::log(1000.0));
+  k_static_tables<<<1, 1024, 0, st>>>(vp, rho, S, nx, nz, npml, NX, ng, dx, (float)std::log(1000.0), isx, isz);
   k_static_zero_first<<<(ng + 255) / 256, 256, 0, st>>>(seis, ng, nt);
 
   Grid<float> g;
@@ -285,7 +317,8 @@ extern "C" int swit_forward_shot_static(int32_t nx, int32_t nz, int32_t npml, in
     k_fwd_p<float><<<grid, block, 0, st>>>(g, sr, src, S + kOffP, S + kOffU, S + kOffW, it, 0);
     k_static_uw<<<grid, block, 0, st>>>(g, rec, S + kOffP, S + kOffU, S + kOffW, seis, it);
   }
-  ce = cudaGetLastError();
+  k_static_poison<<<152, 256, 0, st>>>(S, seis, (size_t)ng * nt);
+  const cudaError_t ce = cudaGetLastError();
   if (ce != cudaSuccess) return fail(SWIT_E_CUDA, "launch: %s", cudaGetErrorString(ce));
   return 0;
 }

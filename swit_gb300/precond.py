@@ -23,29 +23,20 @@ def _gauss_1d(span, dtype, device):
     return (a / a.sum()).to(dtype)
 
 
-_toeplitz = {}
-
-
-def _band(n, k):
-    """(n, n) matrix T with T[i, j] = k[j - i + r] for |j - i| <= r (r = len(k) // 2),
-    so T @ x is the zero-filled 'same' convolution of x with the symmetric k."""
-    key = (n, k.numel(), k.dtype, str(k.device), float(k[0]))
-    T = _toeplitz.get(key)
-    if T is None:
-        r = k.numel() // 2
-        i = torch.arange(n, device=k.device)
-        d = i[None, :] - i[:, None] + r
-        T = torch.where((d >= 0) & (d <= 2 * r), k[d.clamp(0, 2 * r)], torch.zeros((), dtype=k.dtype, device=k.device))
-        if len(_toeplitz) > 64:
-            _toeplitz.clear()
-        _toeplitz[key] = T
-    return T
+def _conv_axis(Z, k):
+    """Zero-filled 'same' convolution of every row of Z (m, n) with the
+    symmetric odd-length k: one (2r+1)-tap stencil pass, O(m n r) work and no
+    n x n operator."""
+    r = k.numel() // 2
+    out = torch.nn.functional.conv1d(Z.reshape(Z.shape[0], 1, Z.shape[1]), k.reshape(1, 1, -1), padding=r)
+    return out.reshape(Z.shape)
 
 
 def _conv_same(Z, k):
-    """scipy.signal.convolve2d(Z, outer(k, k), 'same') with zero fill: one banded
-    matrix product per axis (k symmetric, odd length)."""
-    return _band(Z.shape[0], k) @ Z @ _band(Z.shape[1], k).T
+    """scipy.signal.convolve2d(Z, outer(k, k), 'same') with zero fill, as two
+    separable passes (along z, then along x)."""
+    Z = _conv_axis(Z.contiguous(), k)
+    return _conv_axis(Z.t().contiguous(), k).t()
 
 
 def smooth2d(Z, span=10):

@@ -25,3 +25,6 @@ def test_reference_arm_prints_one_contract_line():
     assert d["cpu_baseline"]["value"] == d["value"]
     assert d["e2e"] == {"value": d["value"], "unit": d["unit"], "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
     assert d["cpu_baseline_with_strip_io"]["value"] > 0
+    # every step is the whole workload, named with the same keys as the GPU arm's config
+    assert d["config"]["shots_per_gpu"] == 2 and d["config"]["nt"] == 40
+    assert "all 2 shots" in d["cpu_baseline"]["sample"]

@@ -1,6 +1,6 @@
 """Device misfits against golden vectors made by the reference's own
-toolbox/misfit.py (tests/golden/make_misfit_golden.py).  Runs on CPU tensors
-here; the same torch code runs on the GPU."""
+toolbox/misfit.py (tests/golden/make_misfit_golden.py), on CPU tensors and
+(marked gpu) on CUDA tensors."""
 import os
 
 import numpy as np
@@ -10,14 +10,18 @@ import torch
 from swit_gb300 import misfit as M
 
 G = np.load(os.path.join(os.path.dirname(__file__), "golden", "misfit_golden.npz"))
+DEVICES = [pytest.param("cpu", id="cpu"), pytest.param("cuda", id="cuda", marks=pytest.mark.gpu)]
 
 
+@pytest.mark.parametrize("device", DEVICES)
 @pytest.mark.parametrize("name", ["waveform", "envelope", "traveltime", "globalcorrelation"])
-def test_adjoint_source_and_value_match_reference(name):
-    syn = torch.from_numpy(G["syn"])
-    obs = torch.from_numpy(G["obs"])
+def test_adjoint_source_and_value_match_reference(name, device):
+    syn = torch.from_numpy(G["syn"]).to(device)
+    obs = torch.from_numpy(G["obs"]).to(device)
     dt = float(G["dt"])
     val, adj = M.adjoint_source(syn, obs, dt, name)
+    assert adj.device.type == device
+    adj = adj.cpu()
     ref = G["adj_" + name]
     scale = np.abs(ref).max()
     assert np.abs(adj.numpy() - ref).max() <= 1e-5 * scale, name
@@ -27,9 +31,10 @@ def test_adjoint_source_and_value_match_reference(name):
     assert not np.any(adj.numpy()[3])
 
 
-def test_cross_correlation_lag_matches_reference():
-    cc = M.cross_correlate_max(torch.from_numpy(G["obs"]), torch.from_numpy(G["syn"]))
-    np.testing.assert_array_equal(cc.numpy(), G["ccmax"])
+@pytest.mark.parametrize("device", DEVICES)
+def test_cross_correlation_lag_matches_reference(device):
+    cc = M.cross_correlate_max(torch.from_numpy(G["obs"]).to(device), torch.from_numpy(G["syn"]).to(device))
+    np.testing.assert_array_equal(cc.cpu().numpy(), G["ccmax"])
 
 
 def test_batched_shapes_give_the_same_adjoint():

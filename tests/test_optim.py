@@ -1,6 +1,6 @@
 """The device optimiser against search directions made by the reference's own
-toolbox/inversion.py (tests/golden/make_optim_golden.py), on CPU tensors; the
-same torch code runs on the GPU."""
+toolbox/inversion.py (tests/golden/make_optim_golden.py), on CPU tensors and
+(marked gpu) on CUDA tensors."""
 import importlib.util
 import os
 
@@ -15,20 +15,23 @@ _spec = importlib.util.spec_from_file_location("_mk", os.path.join(os.path.dirna
                                                                    "make_optim_golden.py"))
 _mk = importlib.util.module_from_spec(_spec)
 _spec.loader.exec_module(_mk)
+DEVICES = [pytest.param("cpu", id="cpu"), pytest.param("cuda", id="cuda", marks=pytest.mark.gpu)]
 
 
+@pytest.mark.parametrize("device", DEVICES)
 @pytest.mark.parametrize("scheme,key", [("LBFGS", "d_lbfgs"), ("NLCG", "d_nlcg")])
-def test_directions_match_reference(scheme, key):
+def test_directions_match_reference(scheme, key, device):
     A, b, v0 = _mk.problem()
-    A, b = torch.from_numpy(A), torch.from_numpy(b)
-    st = O.init_state(scheme, v0.size, device="cpu")
-    st["v_now"] = torch.from_numpy(v0.copy())
-    st["v_old"] = torch.from_numpy(v0.copy())
+    A, b = torch.from_numpy(A).to(device), torch.from_numpy(b).to(device)
+    st = O.init_state(scheme, v0.size, device=device)
+    st["v_now"] = torch.from_numpy(v0.copy()).to(device)
+    st["v_old"] = torch.from_numpy(v0.copy()).to(device)
     for i in range(4):
         st["g_now"] = A @ st["v_now"] - b
         st = O.nlcg_direction(st) if scheme == "NLCG" else O.lbfgs_direction(st)
         ref = G[key][i]
-        np.testing.assert_allclose(st["d_now"].numpy(), ref, rtol=0, atol=2e-5 * np.abs(ref).max())
+        assert st["d_now"].device.type == device
+        np.testing.assert_allclose(st["d_now"].cpu().numpy(), ref, rtol=0, atol=2e-5 * np.abs(ref).max())
         if scheme == "NLCG":
             st["g_old"], st["d_old"] = st["g_now"], st["d_now"]
         else:
@@ -36,19 +39,21 @@ def test_directions_match_reference(scheme, key):
         st["v_now"] = st["v_now"] + 0.5 * st["d_now"]
 
 
+@pytest.mark.parametrize("device", DEVICES)
 @pytest.mark.parametrize("scheme", ["LBFGS", "NLCG"])
-def test_fwi_loop_decreases_a_quadratic(scheme):
+def test_fwi_loop_decreases_a_quadratic(scheme, device):
     A, b, v0 = _mk.problem()
-    A, b = torch.from_numpy(A), torch.from_numpy(b)
+    A, b = torch.from_numpy(A).to(device), torch.from_numpy(b).to(device)
 
     def f(v):
         return 0.5 * v @ (A @ v) - b @ v
 
-    st, hist = O.fwi(torch.from_numpy(v0), lambda v: (f(v), A @ v - b), f, scheme=scheme, maxiter=5,
+    st, hist = O.fwi(torch.from_numpy(v0).to(device), lambda v: (f(v), A @ v - b), f, scheme=scheme, maxiter=5,
                      step_length=0.5, vpmax=1e9, vpmin=-1e9)
     fs = [h["f"] for h in hist]
     assert all(h["ls_status"] == 0 for h in hist)
-    assert fs == sorted(fs, reverse=True) and fs[-1] < float(f(torch.from_numpy(v0)))
+    assert fs == sorted(fs, reverse=True) and fs[-1] < float(f(torch.from_numpy(v0).to(device)))
+    assert st["v_now"].device.type == device
 
 
 def test_model_update_clips_to_bounds():
