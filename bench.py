@@ -46,7 +46,7 @@ def parse():
     ap.add_argument("--branches", type=int, default=0, help="concurrent graph branches (0 = engine default)")
     ap.add_argument("--adjoint", default="fd2dmpi", choices=["fd2dmpi", "exact"],
                     help="fd2dmpi's adjoint (the reference's gradient) or the exact discrete adjoint")
-    ap.add_argument("--kernel", default="auto", choices=["auto", "fused", "split", "vec", "cluster", "hybrid", "band"])
+    ap.add_argument("--kernel", default="auto", choices=["auto", "walk", "split", "vec", "cluster", "hybrid", "band"])
     ap.add_argument("--no-tune", action="store_true", help="skip the launch-configuration autotuner")
     ap.add_argument("--no-extras", action="store_true", help="skip plain path, CPU baseline and kernel profile")
     ap.add_argument("--workload", default="marmousi", choices=["marmousi", "large", "multi", "correlation"],
@@ -92,7 +92,7 @@ def kernel_bytes_per_shot(nx, nz, npml, ng, nt):
         "fwd_uw": 24 * npts + 4 * (9 * nx + 6 * nz) + 4 * ng,  # u, w r/w, p, B; strips, trace samples
         "bwd_uw": 24 * npts + 24 * nint + 4 * (nx + 2 * nz),   # adjoint u, w; reconstruction u, w; strips
         "bwd_p": 20 * npts + 44 * nint + 4 * (5 * nx + 4 * nz) + 4 * ng,  # adjoint p; reco p; imaging; strips
-        # fused: p, u, w, A, B read and p, u, w written once; the interior adds the
+        # walk: p, u, w, A, B read and p, u, w written once; the interior adds the
         # reconstruction state and the three imaging sums
         "fwd_step": 32 * npts + 4 * (9 * nx + 6 * nz) + 4 * ng,
         "bwd_step": 32 * npts + 48 * nint + 4 * (6 * nx + 6 * nz) + 4 * ng,

@@ -74,8 +74,8 @@ typedef struct swit_desc {
                                reverse loop's state in L2, spread evenly over
                                the graph branches; other kernels: all shots)    */
   int32_t block_x;          /* columns per CTA, 0 = automatic: split kernels
-                               1, 2, 4 or 8 (x 32 rows); fused kernels 8, 16
-                               or 32 (x all rows); vec kernels: task lists
+                               1, 2, 4 or 8 (x 32 rows); walk kernels: columns
+                               per tile, 2..256 (default 8); vec kernels: task lists
                                ordered by tiles of block_x columns (a power of
                                two <= 64, default 4) x 256/block_x four-row
                                vectors;
@@ -83,9 +83,11 @@ typedef struct swit_desc {
                                16; the reverse loop takes more CTAs when its six
                                wavefields need them)                            */
   int32_t kernel_variant;   /* 0 = automatic (vec), 1 = split: two kernels per step,
-                               in place, one point per thread; 2 = fused: one
-                               kernel per step, double-buffered (NZ + 2 npml <=
-                               1024); 3 = vec: split, four rows per thread;
+                               in place, one point per thread; 2 = walk: one
+                               kernel per step, double-buffered, each warp
+                               walking a tile of columns with the x-neighbours
+                               in registers and the z-neighbours by shuffle;
+                               3 = vec: split, four rows per thread;
                                4 = cluster: one launch per time loop, one
                                thread-block cluster per shot holding its
                                wavefields in distributed shared memory
@@ -189,7 +191,7 @@ int swit_import_snapshot(swit_engine* e, const float* src, const float* boundary
  * CUDA event pair around it on `stream`, and returns for each kernel --
  * [0] forward pressure phase, [1] forward velocity phase, [2] backward velocity
  * phase, [3] backward pressure phase -- the number of launches and the mean
- * launch duration in milliseconds.  With the fused variant, [0] is the forward
+ * launch duration in milliseconds.  With the walk variant, [0] is the forward
  * step kernel, [2] the reverse step kernel and [1], [3] are unused (0 launches).
  * Synchronises the stream. */
 int swit_profile_kernels(swit_engine* e, int32_t launches[4], double mean_ms[4], void* stream);

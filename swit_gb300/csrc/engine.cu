@@ -18,7 +18,7 @@
 
 #include "../../include/swit_gb300.h"
 #include "kernels.cuh"
-#include "kernels_fused.cuh"
+#include "kernels_walk.cuh"
 #include "kernels_vec.cuh"
 #include "kernels_cluster.cuh"
 #include "kernels_band.cuh"
@@ -63,7 +63,7 @@ struct swit_engine {
   int nx, nz, L, nt, NX, NZ, LD, LDI, fs, fs_flag, ns, ngmax, SL, prec, path;
   float dx32, dt32;
   int batch, bx;
-  int variant;  // 1 = split, 2 = fused (one kernel per step, ping-pong), 3 = vec (split, 4 rows per thread),
+  int variant;  // 1 = split, 2 = walk (one kernel per step, ping-pong), 3 = vec (split, 4 rows per thread),
                 // 4 = cluster (one persistent cluster per shot, wavefields in distributed shared memory),
                 // 5 = hybrid (cluster forward, vec reverse loop), 6 = band (vec bodies on bands of
                 // columns staged through shared memory by bulk copies)
@@ -94,6 +94,7 @@ struct swit_engine {
   // device tables
   int *d_ng = nullptr, *d_isx = nullptr, *d_isz = nullptr, *d_risx = nullptr, *d_risz = nullptr;
   int *d_colptr = nullptr, *d_ig = nullptr, *d_zr = nullptr, *d_live = nullptr, *d_zlo = nullptr, *d_zhi = nullptr;
+  int4* d_rcol = nullptr;  // per shot and column: first receiver entry {ig, row, count, entry}
   double* d_mtrace = nullptr;
   // device arrays of type R (float or double)
   void *A = nullptr, *B = nullptr, *damp = nullptr, *cint = nullptr;
@@ -101,7 +102,7 @@ struct swit_engine {
   void *p = nullptr, *u = nullptr, *w = nullptr, *pb = nullptr, *ub = nullptr, *wb = nullptr;
   void *pe = nullptr, *ue = nullptr, *we = nullptr, *dg = nullptr, *dfw = nullptr, *dbk = nullptr;
   void *strips = nullptr, *src = nullptr, *seis_t = nullptr, *adj_t = nullptr;
-  // second state buffers of the fused variant
+  // second state set of the walk variant
   void *p2 = nullptr, *u2 = nullptr, *w2 = nullptr, *pb2 = nullptr, *ub2 = nullptr, *wb2 = nullptr;
   void *pe2 = nullptr, *ue2 = nullptr, *we2 = nullptr;
   float* d_in = nullptr;     // float staging: sources / obs / adjoint sources from the host
@@ -162,7 +163,7 @@ void release(swit_engine* e) {
     if (e->ev_join[i]) cudaEventDestroy(e->ev_join[i]);
   }
   if (e->ev_fork) cudaEventDestroy(e->ev_fork);
-  void* ptrs[] = {e->d_zlo, e->d_zhi, e->d_ng, e->d_isx, e->d_isz, e->d_risx, e->d_risz, e->d_colptr, e->d_ig, e->d_zr, e->d_live,
+  void* ptrs[] = {e->d_rcol, e->d_zlo, e->d_zhi, e->d_ng, e->d_isx, e->d_isz, e->d_risx, e->d_risz, e->d_colptr, e->d_ig, e->d_zr, e->d_live,
                   e->d_mtrace, e->A, e->B, e->damp, e->cint, e->kp, e->ku, e->kw, e->p, e->u, e->w, e->pb, e->ub, e->wb, e->pe,
                   e->ue, e->we, e->dg, e->dfw, e->dbk, e->strips, e->src, e->seis_t, e->adj_t, e->d_in,
                   e->d_stage, e->p2, e->u2, e->w2, e->pb2, e->ub2, e->wb2, e->pe2, e->ue2, e->we2, e->d_list, e->d_blist, e->d_bcnt, e->d_err, e->ckpt,
@@ -189,9 +190,9 @@ Grid<R> make_grid(const swit_engine* e) {
   g.snt = e->snt;
   g.sit0 = e->sit0;
   g.FSZ = (size_t)e->NX * e->LD;
-  g.FSI = e->variant >= 3 ? g.FSZ : (size_t)e->nx * e->LDI;
+  g.FSI = e->variant >= 2 ? g.FSZ : (size_t)e->nx * e->LDI;
   g.IL = e->IL;
-  if (e->variant >= 3) g.LDI = e->LD;
+  if (e->variant >= 2) g.LDI = e->LD;
   g.dt = (R)e->dt32;
   g.c1 = R(9.0) / R(8.0);    // global.f90:34
   g.c2 = R(-1.0) / R(24.0);  // global.f90:35
@@ -205,7 +206,7 @@ Grid<R> make_grid(const swit_engine* e) {
 }
 
 inline Receivers make_rec(const swit_engine* e) {
-  return Receivers{e->d_colptr, e->d_ig, e->d_zr, e->d_zlo, e->d_zhi, e->rcomp};
+  return Receivers{e->d_colptr, e->d_ig, e->d_zr, e->d_zlo, e->d_zhi, e->rcomp, e->d_rcol};
 }
 inline Sources make_src(const swit_engine* e) { return Sources{e->d_isx, e->d_isz, e->d_risx, e->d_risz}; }
 
@@ -213,64 +214,6 @@ inline Sources make_src(const swit_engine* e) { return Sources{e->d_isx, e->d_is
 inline void stencil_shape(const swit_engine* e, int nb, dim3& grid, dim3& block) {
   block = dim3(32, e->bx, 1);
   grid = dim3((e->NZ + 31) / 32, (e->NX + e->bx - 1) / e->bx, nb);
-}
-
-// One fused forward step (fdcore.f90:77-159) of shots [shot0, shot0+nb).
-template <class R>
-void launch_fwd_step(swit_engine* e, bool store, int shot0, int nb, int it, cudaStream_t st) {
-  Grid<R> g = make_grid<R>(e);
-  const bool even = (it - 2) % 2 == 0;  // step it reads set A when it is even
-  const R* P0 = (const R*)(even ? e->p : e->p2);
-  const R* U0 = (const R*)(even ? e->u : e->u2);
-  const R* W0 = (const R*)(even ? e->w : e->w2);
-  R* P1 = (R*)(even ? e->p2 : e->p);
-  R* U1 = (R*)(even ? e->u2 : e->u);
-  R* W1 = (R*)(even ? e->w2 : e->w);
-  R* strips = store ? (R*)e->strips : nullptr;
-  const dim3 grid((e->NX + e->bx - 1) / e->bx, nb), block(e->LD);
-  const size_t sm = 2 * (size_t)(e->LD + 4) * sizeof(R);
-#define FWD(TX)                                                                                            \
-  k_fwd_step<R, TX><<<grid, block, sm, st>>>(g, make_src(e), make_rec(e), (const R*)e->src, P0, U0, W0, P1, U1, \
-                                             W1, (R*)e->seis_t, strips, it, shot0)
-  if (e->bx == 8)
-    FWD(8);
-  else if (e->bx == 32)
-    FWD(32);
-  else
-    FWD(16);
-#undef FWD
-}
-
-// One fused reverse step (fdcore.f90:220-287, 309-373; solver.f90:232-239).
-template <class R>
-void launch_bwd_step(swit_engine* e, int shot0, int nb, int it, cudaStream_t st) {
-  Grid<R> g = make_grid<R>(e);
-  const bool even = (e->nt - it) % 2 == 0;  // the first reverse step reads set A
-  const R* PB0 = (const R*)(even ? e->pb : e->pb2);
-  const R* UB0 = (const R*)(even ? e->ub : e->ub2);
-  const R* WB0 = (const R*)(even ? e->wb : e->wb2);
-  R* PB1 = (R*)(even ? e->pb2 : e->pb);
-  R* UB1 = (R*)(even ? e->ub2 : e->ub);
-  R* WB1 = (R*)(even ? e->wb2 : e->wb);
-  const R* PE0 = (const R*)(even ? e->pe : e->pe2);
-  const R* UE0 = (const R*)(even ? e->ue : e->ue2);
-  const R* WE0 = (const R*)(even ? e->we : e->we2);
-  R* PE1 = (R*)(even ? e->pe2 : e->pe);
-  R* UE1 = (R*)(even ? e->ue2 : e->ue);
-  R* WE1 = (R*)(even ? e->we2 : e->we);
-  const dim3 grid((e->NX + e->bx - 1) / e->bx, nb), block(e->LD);
-  const size_t sm = 4 * (size_t)(e->LD + 4) * sizeof(R);
-#define BWD(TX)                                                                                                \
-  k_bwd_step<R, TX><<<grid, block, sm, st>>>(g, make_src(e), make_rec(e), (const R*)e->src, (const R*)e->adj_t, \
-                                             PB0, UB0, WB0, PB1, UB1, WB1, PE0, UE0, WE0, PE1, UE1, WE1,         \
-                                             (R*)e->dg, (R*)e->dfw, (R*)e->dbk, (const R*)e->strips, it, shot0)
-  if (e->bx == 8)
-    BWD(8);
-  else if (e->bx == 32)
-    BWD(32);
-  else
-    BWD(16);
-#undef BWD
 }
 
 // Launch with programmatic stream serialization when pdl is set: the next
@@ -346,6 +289,40 @@ void launch_cluster_bwd_t(swit_engine* e, int shot0, int nb, cudaStream_t st) {
                      (R*)e->dbk, (const R*)e->strips, shot0);
 }
 
+// Walk variant (kernels_walk.cuh): one launch per step and batch; a CTA is
+// kWalkWarps of the ceil(LD/4/28) warps of one tile of e->bx columns of one
+// shot (grid: tiles x shots x warp groups).  State is
+// double-buffered: forward step it reads set A (p, u, w) when it is even and
+// set B (p2, u2, w2) when it is odd; reverse step it reads set A when nt - it
+// is even.
+inline dim3 walk_block(const swit_engine*) { return dim3(32, kWalkWarps); }
+inline dim3 walk_grid(const swit_engine* e, int nb) {
+  const int nw = (e->LD / 4 + kWalkOwn - 1) / kWalkOwn;  // warps per column
+  return dim3((e->NX + e->bx - 1) / e->bx, nb, (nw + kWalkWarps - 1) / kWalkWarps);
+}
+
+template <class R>
+void launch_fwd_walk(swit_engine* e, bool store, int shot0, int nb, int it, cudaStream_t st) {
+  Grid<R> g = make_grid<R>(e);
+  const bool a = (it - 2) % 2 == 0;
+  launch_pdl(e->pdl, k_fwd_walk<R>, walk_grid(e, nb), walk_block(e), st, g, make_src(e), make_rec(e),
+             (const R*)e->src, (const R*)(a ? e->p : e->p2), (const R*)(a ? e->u : e->u2),
+             (const R*)(a ? e->w : e->w2), (R*)(a ? e->p2 : e->p), (R*)(a ? e->u2 : e->u), (R*)(a ? e->w2 : e->w),
+             (R*)e->seis_t, store ? (R*)e->strips : (R*)nullptr, it, shot0, e->bx);
+}
+
+template <class R>
+void launch_bwd_walk(swit_engine* e, int shot0, int nb, int it, cudaStream_t st) {
+  Grid<R> g = make_grid<R>(e);
+  const bool a = (e->nt - it) % 2 == 0;
+  launch_pdl(e->pdl, k_bwd_walk<R>, walk_grid(e, nb), walk_block(e), st, g, make_src(e), make_rec(e),
+             (const R*)e->src, (const R*)e->adj_t, (const R*)(a ? e->pb : e->pb2), (const R*)(a ? e->ub : e->ub2),
+             (const R*)(a ? e->wb : e->wb2), (R*)(a ? e->pb2 : e->pb), (R*)(a ? e->ub2 : e->ub),
+             (R*)(a ? e->wb2 : e->wb), (const R*)(a ? e->pe : e->pe2), (const R*)(a ? e->ue : e->ue2),
+             (const R*)(a ? e->we : e->we2), (R*)(a ? e->pe2 : e->pe), (R*)(a ? e->ue2 : e->ue),
+             (R*)(a ? e->we2 : e->we), (R*)e->dg, (R*)e->dfw, (R*)e->dbk, (const R*)e->strips, it, shot0, e->bx);
+}
+
 // Forward time loop of shots [shot0, shot0+nb): fdcore.f90:75-160.
 template <class R>
 void launch_forward_steps(swit_engine* e, bool store, int shot0, int nb, cudaStream_t st, int it_lo = 2,
@@ -390,7 +367,7 @@ void launch_forward_steps(swit_engine* e, bool store, int shot0, int nb, cudaStr
     return;
   }
   if (e->variant == 2) {
-    for (int it = it_lo; it <= it_hi; ++it) launch_fwd_step<R>(e, store, shot0, nb, it, st);
+    for (int it = it_lo; it <= it_hi; ++it) launch_fwd_walk<R>(e, store, shot0, nb, it, st);
     return;
   }
   Grid<R> g = make_grid<R>(e);
@@ -447,7 +424,7 @@ void launch_backward_steps(swit_engine* e, int shot0, int nb, cudaStream_t st, i
     return;
   }
   if (e->variant == 2) {
-    for (int it = it_hi; it >= it_lo; --it) launch_bwd_step<R>(e, shot0, nb, it, st);
+    for (int it = it_hi; it >= it_lo; --it) launch_bwd_walk<R>(e, shot0, nb, it, st);
     return;
   }
   Grid<R> g = make_grid<R>(e);
@@ -473,9 +450,12 @@ inline int fwd_batch(const swit_engine* e) { return e->variant == 5 ? e->ns : e-
 // (reverse step it reads the strips of step it-1; none for the last segment
 // when m k + 2 > nt).  Checkpoint slot m holds (p, u, w) after segment m (the
 // last slot is the final state); the state before segment 0 is zero.
-inline void ckpt_copy(swit_engine* e, int slot, int s0, int nb, bool save, cudaStream_t st) {
+// it_after: the forward step after which the state is saved or restored (the
+// walk variant keeps the state after step it in set B when it is even).
+inline void ckpt_copy(swit_engine* e, int slot, int s0, int nb, bool save, int it_after, cudaStream_t st) {
   const size_t fsz = (size_t)e->NX * e->LD * e->esz;
-  void* f[3] = {e->p, e->u, e->w};
+  const bool b = e->variant == 2 && it_after % 2 == 0;
+  void* f[3] = {b ? e->p2 : e->p, b ? e->u2 : e->u, b ? e->w2 : e->w};
   for (int q = 0; q < 3; ++q) {
     char* c = (char*)e->ckpt + (((size_t)slot * 3 + q) * e->ns + s0) * fsz;
     char* a = (char*)f[q] + (size_t)s0 * fsz;
@@ -489,7 +469,7 @@ void forward_checkpointed(swit_engine* e, int s0, int nb, cudaStream_t st) {
   const int k = e->ckpt_k;
   for (int m = 0; m < e->ckpt_m; ++m) {
     launch_forward_steps<R>(e, false, s0, nb, st, std::max(2, m * k + 1), std::min(e->nt, (m + 1) * k));
-    ckpt_copy(e, m, s0, nb, true, st);
+    ckpt_copy(e, m, s0, nb, true, std::min(e->nt, (m + 1) * k), st);
   }
 }
 
@@ -504,7 +484,7 @@ void backward_checkpointed(swit_engine* e, int s0, int nb, cudaStream_t st) {
   for (int m = e->ckpt_m - 1; m >= 0; --m) {
     if (m * k + 2 > e->nt) continue;
     if (m > 0) {
-      ckpt_copy(e, m - 1, s0, nb, false, st);
+      ckpt_copy(e, m - 1, s0, nb, false, m * k, st);
     } else {
       cudaMemsetAsync((char*)e->p + (size_t)s0 * fsz, 0, (size_t)nb * fsz, st);
       cudaMemsetAsync((char*)e->u + (size_t)s0 * fsz, 0, (size_t)nb * fsz, st);
@@ -559,7 +539,7 @@ void exact_reverse(swit_engine* e, int s0, int nb, cudaStream_t st) {
     const int lo = std::max(2, m * k + 1), hi = std::min(e->nt, (m + 1) * k);
     if (lo > hi) continue;
     if (m > 0) {
-      ckpt_copy(e, m - 1, s0, nb, false, st);
+      ckpt_copy(e, m - 1, s0, nb, false, m * k, st);
     } else {
       cudaMemsetAsync((char*)e->p + (size_t)s0 * fsz, 0, (size_t)nb * fsz, st);
       cudaMemsetAsync((char*)e->u + (size_t)s0 * fsz, 0, (size_t)nb * fsz, st);
@@ -889,9 +869,8 @@ int backward_core(swit_engine* e, void* grad, void* fw, void* bk, int on_device,
   CK(cudaMemsetAsync(e->ub, 0, fb, st));
   CK(cudaMemsetAsync(e->wb, 0, fb, st));
   if (e->variant == 2) {
-    CK(cudaMemsetAsync(e->pb2, 0, fb, st));
-    CK(cudaMemsetAsync(e->ub2, 0, fb, st));
-    CK(cudaMemsetAsync(e->wb2, 0, fb, st));
+    void* z2[] = {e->pb2, e->ub2, e->wb2, e->pe2, e->ue2, e->we2};
+    for (void* q : z2) CK(cudaMemsetAsync(q, 0, fb, st));
   }
   CK(cudaMemsetAsync(e->dg, 0, ib, st));
   CK(cudaMemsetAsync(e->dfw, 0, ib, st));
@@ -1037,8 +1016,8 @@ int set_model_impl(swit_engine* e, const float* vp, const float* rho, cudaStream
       damp[i] = kappa * xa * xa;
     }
   }
-  const int LDI = e->variant >= 3 ? LD : e->LDI, IL = e->IL;
-  const size_t nci = e->variant >= 3 ? (size_t)NX * LD : (size_t)nx * e->LDI;
+  const int LDI = e->variant >= 2 ? LD : e->LDI, IL = e->IL;
+  const size_t nci = e->variant >= 2 ? (size_t)NX * LD : (size_t)nx * e->LDI;
   std::vector<R> A((size_t)NX * LD, R(0)), B((size_t)NX * LD, R(0)), ci(nci, R(1));
   for (int ix = 1; ix <= NX; ++ix)
     for (int iz = 1; iz <= NZ; ++iz) {
@@ -1233,7 +1212,7 @@ int profile_impl(swit_engine* e, int32_t launches[4], double mean_ms[4], cudaStr
     for (int it = 2; it <= e->nt; ++it) {
       if (e->variant == 2) {
         record(0);
-        launch_fwd_step<R>(e, true, s0, nb, it, st);
+        launch_fwd_walk<R>(e, true, s0, nb, it, st);
         record(0);
         continue;
       }
@@ -1291,7 +1270,7 @@ int profile_impl(swit_engine* e, int32_t launches[4], double mean_ms[4], cudaStr
     for (int it = e->nt; it >= 2; --it) {
       if (e->variant == 2) {
         record(2);
-        launch_bwd_step<R>(e, s0, nb, it, st);
+        launch_bwd_walk<R>(e, s0, nb, it, st);
         record(2);
         continue;
       }
@@ -1855,7 +1834,10 @@ void auto_batches(swit_engine* e, int branches) {
   if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, dev) != cudaSuccess ||
       l2 <= 0)
     l2 = 64 << 20;
-  const double state = (3.0 * e->NX * e->NZ + 6.0 * e->nx * e->nz) * e->esz;
+  // reverse-loop state per shot: adjoint fields on the PML grid, reconstruction
+  // fields and imaging sums on the interior; the walk kernels keep two sets
+  const double state = e->variant == 2 ? (6.0 * e->NX * e->NZ + 9.0 * e->nx * e->nz) * e->esz
+                                       : (3.0 * e->NX * e->NZ + 6.0 * e->nx * e->nz) * e->esz;
   const int inflight = std::max(1, (int)(0.7 * l2 / state));
   const int br = std::max(1, std::min(branches ? branches : 3, e->ns));
   const int per_branch = std::max(1, inflight / br);
@@ -1919,21 +1901,17 @@ int swit_create(const swit_desc* d, swit_engine** out) {
     delete e;
     return fail(SWIT_E_ARG, "receiver_component must be 0 (p), 1 (vx) or 2 (vz) (got %d)", d->receiver_component);
   }
-  if (d->receiver_component && e->variant != 3) {
+  if (d->receiver_component && e->variant != 2 && e->variant != 3) {
     delete e;
-    return fail(SWIT_E_ARG, "vx / vz receivers run on the vec kernels (kernel_variant 0 or 3)");
+    return fail(SWIT_E_ARG, "vx / vz receivers run on the walk or vec kernels (kernel_variant 0, 2 or 3)");
   }
   e->rcomp = d->receiver_component;
   if (e->exact) e->SL = e->NX * e->LD;  // the strip buffer holds D of each step
-  if (e->variant == 2 && e->LD > 1024) {
-    delete e;
-    return fail(SWIT_E_LIMIT, "the fused kernels need NZ + 2 npml <= 1024 (got %d)", e->NZ);
-  }
   if (e->variant == 2) {
-    e->bx = d->block_x > 0 ? d->block_x : 16;
-    if (e->bx != 8 && e->bx != 16 && e->bx != 32) {
+    e->bx = d->block_x > 0 ? d->block_x : 8;  // columns per tile
+    if (e->bx < 2 || e->bx > 256) {
       delete e;
-      return fail(SWIT_E_ARG, "block_x of the fused kernels must be 8, 16 or 32");
+      return fail(SWIT_E_ARG, "block_x (columns per tile) of the walk kernels must be 2..256 (got %d)", e->bx);
     }
   } else if (e->variant == 6) {
     int rc6 = e->prec ? setup_band<double>(e, d->block_x) : setup_band<float>(e, d->block_x);
@@ -1961,14 +1939,15 @@ int swit_create(const swit_desc* d, swit_engine** out) {
       return fail(SWIT_E_ARG, "block_x of the split kernels must be a power of two <= 8");
     }
   }
-  e->IL = e->variant >= 3 ? e->L : 0;
+  e->IL = e->variant >= 2 ? e->L : 0;
   if (d->checkpoint_every < 0) {
     delete e;
     return fail(SWIT_E_ARG, "checkpoint_every must be >= 0 (got %d)", d->checkpoint_every);
   }
-  if (d->checkpoint_every > 0 && e->variant != 3 && e->variant != 6) {
+  if (d->checkpoint_every > 0 && e->variant != 2 && e->variant != 3 && e->variant != 6) {
     delete e;
-    return fail(SWIT_E_ARG, "checkpointed recomputation needs the vec or band kernels (kernel_variant 0, 3 or 6)");
+    return fail(SWIT_E_ARG,
+                "checkpointed recomputation needs the walk, vec or band kernels (kernel_variant 0, 2, 3 or 6)");
   }
   e->ckpt_k = std::min(d->checkpoint_every, e->nt);
   if (d->graph_branches < 0 || d->graph_branches > kCapStreamsMax) {
@@ -1982,7 +1961,8 @@ int swit_create(const swit_desc* d, swit_engine** out) {
     const long long v = std::atoll(gn);
     if (v > 0) e->graph_nodes = (size_t)v;
   }
-  if (d->shots_per_batch == 0 && e->path == 0 && e->variant == 3) auto_batches(e, d->graph_branches);
+  if (d->shots_per_batch == 0 && e->path == 0 && (e->variant == 2 || e->variant == 3))
+    auto_batches(e, d->graph_branches);
   e->ckpt_m = e->ckpt_k ? (e->nt + e->ckpt_k - 1) / e->ckpt_k : 0;
   e->snt = e->ckpt_k ? e->ckpt_k : e->nt;
   e->sit0 = 1;
@@ -2062,6 +2042,13 @@ int swit_create(const swit_desc* d, swit_engine** out) {
     e->zhi.push_back(hi);
   }
   const size_t nent = std::max<size_t>(e->ent_ig.size(), 1);
+  std::vector<int4> rcol((size_t)ns * (NX + 2));
+  for (int s = 0; s < ns; ++s)
+    for (int c = 0; c <= NX + 1; ++c) {
+      const int* cp = &e->colptr[(size_t)s * (NX + 2)];
+      const int e0 = cp[c], n = (c <= NX ? cp[c + 1] : e0) - e0;
+      rcol[(size_t)s * (NX + 2) + c] = n ? make_int4(e->ent_ig[e0], e->ent_zr[e0], n, e0) : make_int4(-1, -1, 0, e0);
+    }
   const size_t FSZ = (size_t)e->NX * e->LD, FSI = (size_t)e->nx * e->LDI;
   int rc = 0;
 #define AL(expr)    \
@@ -2076,6 +2063,7 @@ int swit_create(const swit_desc* d, swit_engine** out) {
   AL(dalloc(e, &e->d_risx, ns));
   AL(dalloc(e, &e->d_risz, ns));
   AL(dalloc(e, &e->d_colptr, (size_t)ns * (NX + 2)));
+  AL(dalloc(e, &e->d_rcol, (size_t)ns * (NX + 2)));
   AL(dalloc(e, &e->d_zlo, ns));
   AL(dalloc(e, &e->d_zhi, ns));
   AL(dalloc(e, &e->d_ig, nent));
@@ -2086,8 +2074,8 @@ int swit_create(const swit_desc* d, swit_engine** out) {
   AL(valloc(e, &e->A, FSZ));
   AL(valloc(e, &e->B, FSZ));
   AL(valloc(e, &e->damp, (size_t)L + 1));
-  AL(valloc(e, &e->cint, e->variant >= 3 ? FSZ : FSI));
-  if (e->variant >= 3) {
+  AL(valloc(e, &e->cint, e->variant >= 2 ? FSZ : FSI));
+  if (e->variant >= 2) {
     AL(valloc(e, &e->kp, FSZ));
     AL(valloc(e, &e->ku, FSZ));
     AL(valloc(e, &e->kw, FSZ));
@@ -2095,12 +2083,10 @@ int swit_create(const swit_desc* d, swit_engine** out) {
   void** fields[] = {&e->p, &e->u, &e->w, &e->pb, &e->ub, &e->wb};
   for (void** f : fields) AL(valloc(e, f, (size_t)ns * FSZ));
   void** ifields[] = {&e->pe, &e->ue, &e->we, &e->dg, &e->dfw, &e->dbk};
-  for (void** f : ifields) AL(valloc(e, f, (size_t)ns * (e->variant >= 3 ? FSZ : FSI)));
-  if (e->variant == 2) {
-    void** f2[] = {&e->p2, &e->u2, &e->w2, &e->pb2, &e->ub2, &e->wb2};
+  for (void** f : ifields) AL(valloc(e, f, (size_t)ns * (e->variant >= 2 ? FSZ : FSI)));
+  if (e->variant == 2) {  // second state set of the walk kernels
+    void** f2[] = {&e->p2, &e->u2, &e->w2, &e->pb2, &e->ub2, &e->wb2, &e->pe2, &e->ue2, &e->we2};
     for (void** f : f2) AL(valloc(e, f, (size_t)ns * FSZ));
-    void** i2[] = {&e->pe2, &e->ue2, &e->we2};
-    for (void** f : i2) AL(valloc(e, f, (size_t)ns * FSI));
   }
   AL(valloc(e, &e->strips, (size_t)ns * e->snt * e->SL));
   if (e->ckpt_k) AL(valloc(e, &e->ckpt, (size_t)e->ckpt_m * 3 * ns * FSZ));
@@ -2124,6 +2110,7 @@ int swit_create(const swit_desc* d, swit_engine** out) {
       (rc = h2d(e->d_risx, e->risx.data(), ns * sizeof(int))) ||
       (rc = h2d(e->d_risz, e->risz.data(), ns * sizeof(int))) ||
       (rc = h2d(e->d_colptr, e->colptr.data(), e->colptr.size() * sizeof(int))) ||
+      (rc = h2d(e->d_rcol, rcol.data(), rcol.size() * sizeof(int4))) ||
       (rc = h2d(e->d_zlo, e->zlo.data(), ns * sizeof(int))) || (rc = h2d(e->d_zhi, e->zhi.data(), ns * sizeof(int))) ||
       (e->ent_ig.size() && ((rc = h2d(e->d_ig, e->ent_ig.data(), e->ent_ig.size() * sizeof(int))) ||
                             (rc = h2d(e->d_zr, e->ent_zr.data(), e->ent_zr.size() * sizeof(int)))))) {

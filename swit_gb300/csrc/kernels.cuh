@@ -51,6 +51,9 @@ struct Receivers {
   const int* __restrict__ zlo;  // per shot: lowest and highest receiver row (vectorised kernels;
   const int* __restrict__ zhi;  // may be null elsewhere)
   int comp;                     // recorded component: 0 = p, 1 = vx (u), 2 = vz (w); vec kernels only
+  // per shot and column 0 .. NX+1: {ig, row} of the column's first entry, the
+  // column's entry count and its first entry (walk kernels; may be null elsewhere)
+  const int4* __restrict__ rcol;
 };
 
 struct Sources {

@@ -46,7 +46,7 @@ class Engine:
         if path not in ("batched", "plain"):
             raise ValueError("path must be 'batched' or 'plain'")
         self.path = path
-        variants = {"auto": 0, "split": 1, "fused": 2, "vec": 3, "cluster": 4, "hybrid": 5, "band": 6}
+        variants = {"auto": 0, "split": 1, "walk": 2, "vec": 3, "cluster": 4, "hybrid": 5, "band": 6}
         if adjoint not in ("fd2dmpi", "exact"):
             raise ValueError("adjoint must be 'fd2dmpi' or 'exact'")
         self.adjoint = adjoint
@@ -226,7 +226,7 @@ class Engine:
         _lib.check(self._lib.swit_profile_kernels(self._h, n, ms, torch.cuda.current_stream().cuda_stream))
         names = ("fwd_p", "fwd_uw", "bwd_uw", "bwd_p")
         kind = self.query()["kernel"]
-        if kind == "fused":
+        if kind == "walk":
             names = ("fwd_step", None, "bwd_step", None)
         elif kind == "cluster":
             names = ("fwd_loop", None, "bwd_loop", None)
@@ -241,7 +241,7 @@ class Engine:
                                         C.byref(kv), C.byref(br)))
         return dict(device_bytes=by.value, shots_per_batch=sb.value, block_x=bx.value, graph_branches=br.value,
                     kernels_per_forward=kf.value,
-                    kernels_per_backward=kb.value, kernel={1: "split", 2: "fused", 3: "vec", 4: "cluster", 5: "hybrid", 6: "band"}.get(kv.value, "?"))
+                    kernels_per_backward=kb.value, kernel={1: "split", 2: "walk", 3: "vec", 4: "cluster", 5: "hybrid", 6: "band"}.get(kv.value, "?"))
 
     def check(self):
         """Waits for torch's current stream and raises SwitError if a kernel gave

@@ -127,7 +127,7 @@ def _desc(s, **over):
 @pytest.mark.parametrize("over,code", [
     (dict(nx=4), _lib.SwitError), (dict(npml=1), _lib.SwitError), (dict(nt=1), _lib.SwitError),
     (dict(dx=0.0), _lib.SwitError), (dict(precision=3), _lib.SwitError),
-    (dict(block_x=3, kernel_variant=1), _lib.SwitError), (dict(block_x=12, kernel_variant=2), _lib.SwitError),
+    (dict(block_x=3, kernel_variant=1), _lib.SwitError), (dict(block_x=300, kernel_variant=2), _lib.SwitError),
     (dict(kernel_variant=7), _lib.SwitError), (dict(checkpoint_every=-1), _lib.SwitError),
     (dict(checkpoint_every=5, kernel_variant=1), _lib.SwitError),
     (dict(graph_branches=-1), _lib.SwitError), (dict(graph_branches=5), _lib.SwitError),

@@ -56,7 +56,7 @@ def test_forward_seismograms_match_oracle(base):
     np.testing.assert_array_equal(seis, base["ref"]["seis"])
 
 
-@pytest.mark.parametrize("kernel", ["split", "vec", "cluster", "band"])
+@pytest.mark.parametrize("kernel", ["split", "walk", "vec", "cluster", "band"])
 def test_boundary_strips_and_end_states_match_oracle(base, kernel):
     s = base["s"]
     with engine(s, kernel=kernel) as e:
@@ -93,8 +93,8 @@ def test_gradient_l2_single_call_matches_oracle(base):
     assert abs(out["misfit"] - want) <= 1e-6 * want
 
 
-@pytest.mark.parametrize("opts", [dict(path="plain"), dict(shots_per_batch=2), dict(kernel="fused", block_x=8),
-                                  dict(kernel="fused", block_x=32), dict(kernel="fused", path="plain"),
+@pytest.mark.parametrize("opts", [dict(path="plain"), dict(shots_per_batch=2), dict(kernel="walk", block_x=8),
+                                  dict(kernel="walk", block_x=32), dict(kernel="walk", path="plain"),
                                   dict(kernel="split"), dict(kernel="split", block_x=8),
                                   dict(kernel="split", block_x=1), dict(kernel="split", path="plain"),
                                   dict(kernel="split", shots_per_batch=2), dict(kernel="vec"),
@@ -126,7 +126,7 @@ def test_launch_variants_are_identical(base, opts):
     np.testing.assert_array_equal(bk, base["grad"]["bk"])
 
 
-@pytest.mark.parametrize("kernel", ["fused", "split", "vec", "cluster", "band"])
+@pytest.mark.parametrize("kernel", ["walk", "split", "vec", "cluster", "band"])
 def test_fp64_build_matches_fp64_oracle(base, kernel):
     s, pb = base["s"], base["pb"]
     ref = O.forward(pb, s.vp_true, base["rho"], base["src"], store=True, fp64=True)
@@ -151,7 +151,7 @@ def test_repeated_backward_after_one_forward(base):
     np.testing.assert_array_equal(g2, base["grad"]["g"])
 
 
-@pytest.mark.parametrize("kernel", ["fused", "split", "vec", "cluster", "band"])
+@pytest.mark.parametrize("kernel", ["walk", "split", "vec", "cluster", "band"])
 def test_edge_geometry_surface_receivers_deep_source_uneven_traces(kernel):
     """Receivers on z = 0 (moved one node down), a source deep enough that the
     reconstruction subtracts it (fdcore.f90:250-256), shots with different
@@ -179,7 +179,7 @@ def test_edge_geometry_surface_receivers_deep_source_uneven_traces(kernel):
     np.testing.assert_array_equal(bk, gref["bk"])
 
 
-@pytest.mark.parametrize("kernel", ["fused", "split", "vec", "cluster", "band"])
+@pytest.mark.parametrize("kernel", ["walk", "split", "vec", "cluster", "band"])
 def test_no_free_surface(kernel):
     s, _ = case(nt=200)
     s.free_surface = 0
@@ -228,7 +228,7 @@ def test_state_and_model_errors(base):
             e.backward(base["adj"])
 
 
-@pytest.mark.parametrize("kernel", ["vec", "cluster", "band"])
+@pytest.mark.parametrize("kernel", ["walk", "vec", "cluster", "band"])
 @pytest.mark.parametrize("npml", [8, 9, 10, 11])
 def test_vec_kernels_every_mirror_alignment(npml, kernel):
     """The vectorised kernels own 4 rows per thread; npml mod 4 decides whether
@@ -250,7 +250,7 @@ def test_vec_kernels_every_mirror_alignment(npml, kernel):
     np.testing.assert_array_equal(bk, gref["bk"])
 
 
-@pytest.mark.parametrize("kernel", ["vec", "split", "fused", "cluster", "band"])
+@pytest.mark.parametrize("kernel", ["vec", "split", "walk", "cluster", "band"])
 def test_import_snapshot_replaces_the_forward_run(base, kernel):
     """The adjoint job from saved files (fd2dmpi/solver.f90:212-228): export the
     strips and end states, load them into a fresh engine, run only the reverse loop."""
@@ -279,7 +279,10 @@ def test_cluster_variant_rejects_a_grid_that_does_not_fit_on_chip():
                                   dict(checkpoint_every=298), dict(checkpoint_every=299),
                                   dict(checkpoint_every=1000), dict(checkpoint_every=13, shots_per_batch=2),
                                   dict(checkpoint_every=13, shots_per_batch=1, graph_branches=3),
-                                  dict(checkpoint_every=13, path="plain"), dict(checkpoint_every=13, kernel="band")])
+                                  dict(checkpoint_every=13, path="plain"), dict(checkpoint_every=13, kernel="band"),
+                                  dict(checkpoint_every=1, kernel="walk"), dict(checkpoint_every=13, kernel="walk"),
+                                  dict(checkpoint_every=298, kernel="walk"),
+                                  dict(checkpoint_every=13, kernel="walk", shots_per_batch=1, graph_branches=3)])
 def test_checkpointed_recomputation_gives_the_boundary_saving_results(base, opts):
     """Checkpoints every k steps instead of strips; the reverse loop re-runs each
     segment to regenerate its strips, so every output is bit-identical to the
@@ -408,12 +411,13 @@ def vel():
     return dict(s=s, src=src, rho=rho, out=out)
 
 
+@pytest.mark.parametrize("kernel", ["vec", "walk"])
 @pytest.mark.parametrize("comp", ["vx", "vz"])
 @pytest.mark.parametrize("opts", [dict(), dict(path="plain"), dict(shots_per_batch=1, graph_branches=3),
                                   dict(checkpoint_every=40), dict(precision="fp64")])
-def test_velocity_receivers_match_oracle(vel, comp, opts):
+def test_velocity_receivers_match_oracle(vel, comp, opts, kernel):
     s, o = vel["s"], vel["out"][comp]
-    with engine(s, kernel="vec", receiver_component=comp, **opts) as e:
+    with engine(s, kernel=kernel, receiver_component=comp, **opts) as e:
         e.set_model(s.vp_true, vel["rho"])
         seis = e.forward(vel["src"], save_boundary=True)
         g, fw, bk = e.backward(o["adj"])
@@ -465,3 +469,31 @@ def test_benchmark_configurations_match_oracle(idx, ns, nt):
     assert rel(out["seis"], ref["seis"]) <= SEIS_TOL
     for mine, k in ((out["grad"], "g"), (out["illum_fw"], "fw"), (out["illum_bk"], "bk")):
         assert rel(mine, ref[k]) <= GRAD_TOL, k
+
+
+@pytest.mark.parametrize("block_x", [2, 3, 5, 16, 64])
+@pytest.mark.parametrize("nz,npml", [(28, 9), (210, 10)])
+def test_walk_tiles_narrower_than_the_halo_and_tall_columns(block_x, nz, npml):
+    """Walk kernels: tiles of 2..64 columns (narrower than the 3-column halo of
+    the x-stencils, and wider than the grid) and columns of 56 or 64 vectors
+    (two warps, or three warps in two warp groups with an idle fourth warp):
+    seismograms, strips, end states and gradient equal the oracle's."""
+    s = survey.small(nx=37, nz=nz, npml=npml, nt=150, ns=3, zs=60.0, zr=0.0)
+    pb = O.Problem(s.nx, s.nz, s.npml, s.nt, s.dx, s.dt, s.src_xz, s.rec_xz)
+    src = s.source()
+    rho = s.rho(s.vp_true)
+    ref = O.forward(pb, s.vp_true, rho, src, store=True)
+    adj = np.random.default_rng(block_x).standard_normal(ref["seis"].shape).astype(np.float32)
+    gref = O.adjoint(pb, s.vp_true, rho, src, adj, ref)
+    with engine(s, kernel="walk", block_x=block_x) as e:
+        e.set_model(s.vp_true, rho)
+        seis = e.forward(src, save_boundary=True)
+        snap = e.export_snapshot()
+        g, fw, bk = e.backward(adj)
+        e.check()
+    np.testing.assert_array_equal(seis, ref["seis"])
+    for k in ("boundary", "p_end", "u_end", "w_end"):
+        np.testing.assert_array_equal(snap[k], ref[k], err_msg=k)
+    np.testing.assert_array_equal(g, gref["g"])
+    np.testing.assert_array_equal(fw, gref["fw"])
+    np.testing.assert_array_equal(bk, gref["bk"])
