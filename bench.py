@@ -111,17 +111,25 @@ def measured_peak():
     return 6800.0, "fallback"
 
 
-def ncu_traffic():
-    """DRAM bytes per shot and launch of each stencil kernel from the committed
-    ncu summary (profiles/stencil_traffic.txt), or {} if there is none."""
-    p = os.path.join(ROOT, "profiles", "stencil_traffic.txt")
-    out = {}
-    if os.path.exists(p):
-        for line in open(p):
-            if line.startswith("traffic "):
-                kv = dict(x.split("=", 1) for x in line.split()[1:])
-                out[(kv["kernel"], kv.get("variant"))] = float(kv["bytes_per_shot_launch"])
-    return out
+# DRAM traffic of k_bwd_p_v per shot and launch with the L2 warm: 51,527 B (the average of two steady 9-shot
+# launches, 464 KB each), from
+#   ncu --metrics dram__bytes_read.sum,dram__bytes_write.sum,gpu__time_duration.sum --clock-control none \
+#       -k regex:k_bwd_p_v -s 600 -c 3 --csv \
+#       python bench.py --shots 27 --nt 300 --steps 1 --warmup 1 --no-extras --no-tune --kernel vec
+# (profiles/stencil_traffic.txt keeps the capture's summary).  It is a stored figure, not measured by this run.
+BWD_P_TRAFFIC_PER_SHOT = 51527
+
+
+def l2_bandwidth():
+    """L2 read+write bandwidth (GB/s) measured now on this GPU (swit_l2_bandwidth), or None."""
+    import ctypes as C
+
+    import torch
+
+    from swit_gb300 import _lib
+    g = C.c_double(0.0)
+    rc = _lib.load().swit_l2_bandwidth(64 << 20, 200, C.byref(g), torch.cuda.current_stream().cuda_stream)
+    return g.value if rc == 0 else None
 
 
 # --------------------------------------------------------------------- clocks
@@ -464,26 +472,41 @@ def run_mine(args):
         "gradient_l2": float(np.linalg.norm(gh.astype(np.float64)))}
 
     if not args.no_extras:
-        # per-kernel launch durations (CUDA events around every launch)
+        # per-kernel cost under graph conditions (swit_profile_kernels: each vec kernel alone in a graph of
+        # the loop's batches and branches), the L2 roof, and the dominant kernel against both roofs
         prof = eng.profile_kernels()
         kb = kernel_bytes_per_shot(sv.nx, sv.nz, sv.npml, sv.ng, sv.nt)
         nbatch = -(-per_rank // q["shots_per_batch"])
-        ngroup = -(-nbatch // max(1, q["graph_branches"])) if q["kernel"] == "vec" else nbatch
-        # vec: one timed launch is a group of graph_branches batches launched together on
-        # the graph's concurrent branches (as the captured graphs run them)
-        shots_launch = per_rank / ngroup  # mean shots per timed launch (the last batch may be smaller)
-        tot = {k: v["launches"] * v["mean_ms"] for k, v in prof.items()}
-        top = max(tot, key=tot.get)
+        shots_launch = per_rank / nbatch  # mean shots per launch (the last batch may be smaller)
+        vec = q["kernel"] == "vec"
+        kern = {}
+        for k, v in prof.items():
+            per_step = v["mean_ms"] * (nbatch if vec else v["launches"] / (sv.nt - 1))
+            kern[k] = dict(v, ms_per_time_step=per_step, ms_per_gradient=per_step * (sv.nt - 1))
+        tot = sum(x["ms_per_gradient"] for x in kern.values())
+        for k in kern:
+            kern[k]["share"] = kern[k]["ms_per_gradient"] / tot
+        top = max(kern, key=lambda k: kern[k]["ms_per_gradient"])
         alg = kb[top] * shots_launch
         achieved = alg / (prof[top]["mean_ms"] / 1000.0) / 1e9
-        traffic = ncu_traffic().get((top, q["kernel"]))
+        l2 = l2_bandwidth()
+        traffic = BWD_P_TRAFFIC_PER_SHOT * shots_launch if (top == "bwd_p" and vec) else None
         line["roofline"] = {"bound": "hbm", "kernel": top, "achieved": achieved, "peak": peak, "unit": "GB/s",
                             "frac": achieved / peak, "peak_kind": peak_kind,
-                            "traffic": traffic * shots_launch if traffic else None,
+                            "traffic": traffic,
+                            "traffic_source": "stored: ncu dram__bytes_read.sum + dram__bytes_write.sum of k_bwd_p_v, "
+                                              "%d B per shot and launch (warm L2), scaled by shots per launch"
+                                              % BWD_P_TRAFFIC_PER_SHOT if traffic else None,
+                            "l2_peak": l2, "l2_frac": achieved / l2 if l2 else None,
+                            "l2_peak_source": "measured in this run: swit_l2_bandwidth, read-modify-write sweeps "
+                                              "over 64 MiB through L2",
                             "algorithmic_bytes_per_launch": alg, "mean_launch_ms": prof[top]["mean_ms"],
                             "shots_per_launch": shots_launch,
-                            "concurrent_batches_per_launch": q["graph_branches"] if q["kernel"] == "vec" else 1,
-                            "kernels": {k: dict(v, share=tot[k] / sum(tot.values())) for k, v in prof.items()}}
+                            "timing": ("each kernel alone in a CUDA graph of every batch on the loop's %d branches, "
+                                       "events around one replay" % q["graph_branches"]) if vec else
+                                      "events around every launch",
+                            "kernels": kern, "kernels_ms_per_gradient": tot,
+                            "ms_per_step": ms_per_step}
         # plain one-shot-per-launch path on a bounded sample
         nplain = min(4, per_rank)
         pe = Engine(sv.nx, sv.nz, sv.npml, sv.nt, sv.dx, sv.dt, src_xz[:nplain], rec_xz[:nplain], path="plain",

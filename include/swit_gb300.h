@@ -184,16 +184,28 @@ int swit_export_snapshot(swit_engine* e, void* boundary, void* p_end, void* u_en
 int swit_import_snapshot(swit_engine* e, const float* src, const float* boundary, const float* p_end,
                          const float* u_end, const float* w_end, int on_device, void* stream);
 
-/* Profiling hook (the reference has none; fd2dmpi only prints banners,
- * fd2dmpi/solver.f90:78-84).  Re-runs the forward loop (with strips) and the
- * reverse loop on the inputs staged by the last swit_gradient_l2 or
- * swit_forward + swit_backward, launching every stencil kernel directly with a
- * CUDA event pair around it on `stream`, and returns for each kernel --
- * [0] forward pressure phase, [1] forward velocity phase, [2] backward velocity
- * phase, [3] backward pressure phase -- the number of launches and the mean
- * launch duration in milliseconds.  With the walk variant, [0] is the forward
- * step kernel, [2] the reverse step kernel and [1], [3] are unused (0 launches).
+/* No counterpart in the reference: a measurement utility for the roofline of
+ * the stencil kernels, whose per-step state stays in the L2.  Times `reps`
+ * read-modify-write sweeps (16-byte words, loads and stores through L2 only)
+ * over a device buffer of `bytes` bytes (allocated and freed here) on `stream`
+ * and returns the bytes read plus written per second in GB/s; a buffer well
+ * under the L2 size (e.g. 64 MiB of the GB300's 126 MB) gives the L2 bandwidth.
  * Synchronises the stream. */
+int swit_l2_bandwidth(int64_t bytes, int32_t reps, double* gbs, void* stream);
+
+/* Profiling hook (the reference has none; fd2dmpi only prints banners,
+ * fd2dmpi/solver.f90:78-84).  For each stencil kernel -- [0] forward pressure
+ * phase, [1] forward velocity phase, [2] backward velocity phase, [3] backward
+ * pressure phase -- returns the number of launches timed and the mean time per
+ * launch in milliseconds.  Batched vec engines time each kernel under the
+ * conditions of the captured loop: one graph of that kernel alone, min(nt-1,
+ * 256) steps of every batch on the graph branches, CUDA events around one
+ * replay, so mean_ms x (batches per step) is the kernel's time per step and the
+ * four add up to about the loop's.  Other engines launch every kernel of a
+ * forward and reverse loop with an event pair around it.  With the walk
+ * variant, [0] is the forward step kernel, [2] the reverse step kernel and [1],
+ * [3] are unused (0 launches).  Leaves the wavefields undefined until the next
+ * forward run; synchronises the stream. */
 int swit_profile_kernels(swit_engine* e, int32_t launches[4], double mean_ms[4], void* stream);
 
 /* Capacity of swit_forward_shot_static's fixed scratch (about 2.7 MB per GPU). */

@@ -17,7 +17,7 @@ ERRORS = {-1: "SWIT_E_ARG", -2: "SWIT_E_GEOM", -3: "SWIT_E_CFL", -4: "SWIT_E_MOD
 EXPORTS = ("swit_create", "swit_set_model", "swit_forward", "swit_backward", "swit_gradient_l2",
            "swit_export_snapshot", "swit_import_snapshot", "swit_profile_kernels", "swit_backward_exact", "swit_query", "swit_destroy", "swit_last_error", "swit_damp_profile",
            "swit_forward_shot_static", "swit_check", "swit_misfit_l2", "swit_multi_create", "swit_multi_engine",
-           "swit_multi_gradient_l2", "swit_multi_misfit_l2", "swit_multi_destroy")
+           "swit_multi_gradient_l2", "swit_multi_misfit_l2", "swit_multi_destroy", "swit_l2_bandwidth")
 
 
 class SwitDesc(C.Structure):
@@ -74,6 +74,7 @@ def load(build_if_missing: bool = True):
         "swit_multi_destroy": ([vp], i),
         "swit_last_error": ([], C.c_char_p),
         "swit_damp_profile": ([C.c_int32, C.c_int32, C.c_int32, C.c_float, C.c_float, vp], i),
+        "swit_l2_bandwidth": ([C.c_int64, C.c_int32, C.POINTER(C.c_double), vp], i),
         "swit_forward_shot_static": ([C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_float, C.c_float, C.c_int32,
                                       C.c_float, C.c_float, C.c_int32, vp, vp, vp, vp, vp, vp, vp], i),
     }

@@ -10,8 +10,8 @@ reference's vp kernel g = -2/c sum_t p_f (p_b(t+1) - p_b(t))
 (fd2dmpi/solver.f90:237, 270) divided by dt.  The reference's adjoint injects
 dt * r (fdcore.f90:351-356), so g/dt approximates dL/dvp; it is the
 continuous-adjoint imaging gradient of fd2dmpi, not the exact transpose of the
-discrete forward map (the central finite-difference agreement is measured by
-tests/test_gpu_autograd.py).
+discrete forward map (its agreement with central finite differences is
+measured by tests/test_gpu_solver.py and tests/test_gpu_correlation.py).
 
 With an engine created with adjoint="exact" the backward is the exact
 transpose of the discrete forward map instead (swit_backward_exact): vp.grad

@@ -1,8 +1,8 @@
 """Launch-configuration autotuner.
 
 Times a short Waveform-gradient run (the full geometry and shot count, a few
-dozen time steps) for each candidate (kernel variant, columns per CTA, shots
-per launch, concurrent graph branches) and returns the fastest.  Every candidate computes bit-identical
+dozen time steps) for each candidate (shots per launch, concurrent graph
+branches of the vec kernels) and returns the fastest.  Every candidate computes bit-identical
 results, so the choice only affects speed.  Results are cached per process
 by problem shape.
 """
@@ -16,28 +16,20 @@ from .engine import Engine
 _cache = {}
 
 
-FUSED = False  # the fused kernels are slower on GB300 at every measured shape
-
-
-def candidates(ns, nz_pml):
-    """Launch configurations to time for ns shots (nz_pml: padded rows, for the fused kernels' limit)."""
-    out = []
-    batches = sorted({ns, max(1, (ns + 1) // 2), max(1, (ns + 3) // 4)}, reverse=True)
-    if FUSED and nz_pml <= 1024:
-        for tx in (8, 16, 32):
-            for b in batches:
-                out.append(dict(kernel="fused", block_x=tx, shots_per_batch=b))
-    # vec: the engine's automatic choice (L2-sized batches on three branches), then
-    # 1..8 batches on 1..4 concurrent graph branches (no more branches than batches)
-    out.append(dict(kernel="vec", block_x=4, shots_per_batch=0, graph_branches=0))
+def candidates(ns, nz_pml=None):
+    """Launch configurations to time for ns shots: the vec kernels with the
+    engine's automatic choice (L2-sized batches on three branches), then 1..8
+    batches on 1..4 concurrent graph branches (no more branches than batches).
+    The other variants compute the same bits but measured slower at every shape
+    timed on GB300 (481x141, 49 shots: split 40.8, walk 70.8, cluster 77.7,
+    hybrid 88.3, band 52.2 shot-gradients/s against 125-128 for vec), so they
+    are not timed; name one in Engine(kernel=...) to use it."""
+    out = [dict(kernel="vec", block_x=4, shots_per_batch=0, graph_branches=0)]
     vb = sorted({-(-ns // k) for k in range(1, 9)}, reverse=True)
     for br in (1, 2, 3, 4):
         for b in vb:
             if br == 1 or br <= -(-ns // b):
                 out.append(dict(kernel="vec", block_x=4, shots_per_batch=b, graph_branches=br))
-    out.append(dict(kernel="split", block_x=4, shots_per_batch=ns))
-    out.append(dict(kernel="cluster", block_x=8, shots_per_batch=ns))
-    out.append(dict(kernel="hybrid", block_x=8, shots_per_batch=max(1, (ns + 1) // 2)))
     return out
 
 
@@ -51,7 +43,7 @@ def tune(nx, nz, npml, dx, dt, src_xz, rec_xz, vp, rho, free_surface=1, trial_st
     key = (nx, nz, npml, ns, rec_xz.shape[-2], trial_steps, free_surface, adjoint)
     if key in _cache and cands is None:
         return _cache[key]
-    cands = cands or candidates(ns, nz + 2 * npml)
+    cands = cands or candidates(ns)
     if adjoint == "exact":  # the exact adjoint runs on the vec kernels
         cands = [c for c in cands if c["kernel"] == "vec"]
     nt = trial_steps

@@ -643,6 +643,14 @@ inline bool caller_capturing(cudaStream_t st) {
 
 template <class F>
 int issue_into_capture(swit_engine* e, cudaStream_t st, int nbatch, F&& issue) {
+  // the caller's graph gets every node of the loop: keep it under the same bound
+  // as the engine's own graphs
+  const size_t nodes = (size_t)nbatch * loop_nodes(e);
+  if (nodes > e->graph_nodes)
+    return fail(SWIT_E_LIMIT,
+                "capturing this loop into the caller's graph would add about %zu kernel nodes, above the %zu-node "
+                "bound of one graph; run it uncaptured (the engine then splits it into bounded graphs itself)",
+                nodes, e->graph_nodes);
   capture_fork(e, st);
   for (int b = 0; b < nbatch; ++b) issue(b, capture_stream(e, b, st));
   capture_join(e, st);
@@ -1095,96 +1103,74 @@ int export_impl(swit_engine* e, void* boundary, void* pend, void* uend, void* we
 }
 
 // Per-launch timing of the stencil kernels with CUDA events.
-// Launch profile of the vec kernels as the graphs run them: the batches of a
-// group of `branches` consecutive batches are launched together on the
-// branches' streams (forked from and joined to `st`), and one timed launch is
-// the whole group, CUDA events on `st` around fork and join.
+//
+// Per-kernel cost under the conditions of the captured loop: for each of the
+// four vec kernels, one graph holding only that kernel's launches -- S steps of
+// every batch, batches round-robin on the graph branches as in capture_chunked
+// -- timed with CUDA events around one replay.  mean_ms = replay time / launches,
+// so mean_ms x (batches per step) is the kernel's time per step, and the four
+// kernels' times per step add up to about the loop's time per step (the other
+// kernels of a step are absent from each graph, so their overlap is not).  The
+// wavefields are left with meaningless values; every forward starts from zero.
 template <class R>
-int profile_vec_groups(swit_engine* e, int32_t launches[4], double mean_ms[4], cudaStream_t st) {
+int profile_vec_graphs(swit_engine* e, int32_t launches[4], double mean_ms[4], cudaStream_t st) {
   Grid<R> g = make_grid<R>(e);
   const int B = e->batch, nbatch = (e->ns + B - 1) / B;
-  const int br = std::min(e->branches, nbatch);
-  std::vector<cudaEvent_t> ev[4];
-  auto record = [&](int which) {
-    cudaEvent_t a;
-    cudaEventCreate(&a);
-    ev[which].push_back(a);
-    cudaEventRecord(a, st);
-  };
-  auto fork = [&](int gn) {
-    cudaEventRecord(e->ev_fork, st);
-    for (int i = 0; i < gn - 1; ++i) cudaStreamWaitEvent(e->capx[i], e->ev_fork, 0);
-  };
-  auto join = [&](int gn) {
-    for (int i = 0; i < gn - 1; ++i) {
-      cudaEventRecord(e->ev_join[i], e->capx[i]);
-      cudaStreamWaitEvent(st, e->ev_join[i], 0);
+  const int S = std::min(e->nt - 1, 256);
+  cudaEvent_t t0 = nullptr, t1 = nullptr;
+  CK(cudaEventCreate(&t0));
+  CK(cudaEventCreate(&t1));
+  int rc = 0;
+  for (int k = 0; k < 4 && !rc; ++k) {
+    auto issue = [&](int b, cudaStream_t cs) {
+      const int s0 = b * B, nb = std::min(B, e->ns - s0);
+      for (int i = 0; i < S; ++i) {
+        const int it = k < 2 ? 2 + i : e->nt - i;
+        if (k == 0)
+          launch_pdl(e->pdl, k_fwd_p_v<R>, vec_grid(e, 0, nb), vec_block(e), cs, g, vec_list(e, 0), make_src(e),
+                     (const R*)e->src, (R*)e->p, (const R*)e->u, (const R*)e->w, it, s0);
+        else if (k == 1)
+          launch_pdl(e->pdl, k_fwd_uw_v<R>, vec_grid(e, 1, nb), vec_block(e), cs, g, vec_list(e, 1), make_rec(e),
+                     (const R*)e->p, (R*)e->u, (R*)e->w, (R*)e->seis_t, (R*)e->strips, it, s0);
+        else if (k == 2)
+          launch_pdl(e->pdl, k_bwd_uw_v<R>, vec_grid(e, 2, nb), vec_block(e), cs, g, vec_list(e, 2),
+                     (const R*)e->pb, (R*)e->ub, (R*)e->wb, (const R*)e->pe, (R*)e->ue, (R*)e->we,
+                     (const R*)e->strips, it, s0);
+        else
+          launch_pdl(e->pdl, k_bwd_p_v<R>, vec_grid(e, 3, nb), vec_block(e), cs, g, vec_list(e, 3), make_rec(e),
+                     make_src(e), (const R*)e->src, (const R*)e->adj_t, (R*)e->pb, (const R*)e->ub,
+                     (const R*)e->wb, (R*)e->pe, (const R*)e->ue, (const R*)e->we, (R*)e->dg, (R*)e->dfw,
+                     (R*)e->dbk, (const R*)e->strips, it, s0);
+      }
+    };
+    std::vector<cudaGraphExec_t> ex;
+    const size_t saved = e->graph_nodes;
+    e->graph_nodes = (size_t)(nbatch + 1) * S;  // one graph per kernel (all batches in one chunk)
+    rc = capture_chunked(e, ex, nbatch, (size_t)S, "profile", issue);
+    e->graph_nodes = saved;
+    if (rc) break;
+    float ms = 0.f;
+    if ((rc = launch_graphs(ex, st)) == 0) {  // warm-up replay
+      cudaEventRecord(t0, st);
+      rc = launch_graphs(ex, st);
+      cudaEventRecord(t1, st);
+      cudaError_t ce = cudaEventSynchronize(t1);
+      if (!rc && ce != cudaSuccess) rc = fail(SWIT_E_CUDA, "profile: %s", cudaGetErrorString(ce));
+      if (!rc) cudaEventElapsedTime(&ms, t0, t1);
     }
-  };
-  auto group = [&](int which, int b0, int gn, int it) {
-    record(which);
-    fork(gn);
-    for (int j = 0; j < gn; ++j) {
-      const int s0 = (b0 + j) * B, nb = std::min(B, e->ns - s0);
-      cudaStream_t cs = j ? e->capx[j - 1] : st;
-      if (which == 0)
-        k_fwd_p_v<R><<<vec_grid(e, 0, nb), vec_block(e), 0, cs>>>(g, vec_list(e, 0), make_src(e), (const R*)e->src,
-                                                                (R*)e->p, (const R*)e->u, (const R*)e->w, it, s0);
-      else if (which == 1)
-        k_fwd_uw_v<R><<<vec_grid(e, 1, nb), vec_block(e), 0, cs>>>(g, vec_list(e, 1), make_rec(e), (const R*)e->p,
-                                                                 (R*)e->u, (R*)e->w, (R*)e->seis_t,
-                                                                 (R*)e->strips, it, s0);
-      else if (which == 2)
-        k_bwd_uw_v<R><<<vec_grid(e, 2, nb), vec_block(e), 0, cs>>>(g, vec_list(e, 2), (const R*)e->pb, (R*)e->ub,
-                                                                 (R*)e->wb, (const R*)e->pe, (R*)e->ue, (R*)e->we,
-                                                                 (const R*)e->strips, it, s0);
-      else
-        k_bwd_p_v<R><<<vec_grid(e, 3, nb), vec_block(e), 0, cs>>>(
-            g, vec_list(e, 3), make_rec(e), make_src(e), (const R*)e->src, (const R*)e->adj_t, (R*)e->pb,
-            (const R*)e->ub, (const R*)e->wb, (R*)e->pe, (const R*)e->ue, (const R*)e->we, (R*)e->dg, (R*)e->dfw,
-            (R*)e->dbk, (const R*)e->strips, it, s0);
-    }
-    join(gn);
-    record(which);
-  };
-  const size_t fb = (size_t)e->ns * g.FSZ * e->esz, ib = (size_t)e->ns * g.FSI * e->esz;
-  for (void* q : {e->p, e->u, e->w}) CK(cudaMemsetAsync(q, 0, fb, st));
-  for (int b0 = 0; b0 < nbatch; b0 += br)
-    for (int it = 2; it <= e->nt; ++it) {
-      group(0, b0, std::min(br, nbatch - b0), it);
-      group(1, b0, std::min(br, nbatch - b0), it);
-    }
-  for (void* q : {e->pb, e->ub, e->wb}) CK(cudaMemsetAsync(q, 0, fb, st));
-  CK(cudaMemsetAsync(e->dg, 0, ib, st));
-  CK(cudaMemsetAsync(e->dfw, 0, ib, st));
-  CK(cudaMemsetAsync(e->dbk, 0, ib, st));
-  copy_end<R>(e, st);
-  for (int b0 = 0; b0 < nbatch; b0 += br)
-    for (int it = e->nt; it >= 2; --it) {
-      group(2, b0, std::min(br, nbatch - b0), it);
-      group(3, b0, std::min(br, nbatch - b0), it);
-    }
-  CK(cudaGetLastError());
-  CK(cudaStreamSynchronize(st));
-  for (int q = 0; q < 4; ++q) {
-    double tot = 0.0;
-    const size_t n = ev[q].size() / 2;
-    for (size_t i = 0; i < n; ++i) {
-      float ms = 0.f;
-      cudaEventElapsedTime(&ms, ev[q][2 * i], ev[q][2 * i + 1]);
-      tot += ms;
-    }
-    for (cudaEvent_t x : ev[q]) cudaEventDestroy(x);
-    launches[q] = (int32_t)n;
-    mean_ms[q] = n ? tot / n : 0.0;
+    destroy_graphs(ex);
+    launches[k] = nbatch * S;
+    mean_ms[k] = (double)ms / (nbatch * S);
   }
-  return 0;
+  cudaEventDestroy(t0);
+  cudaEventDestroy(t1);
+  return rc;
 }
 
 template <class R>
 int profile_impl(swit_engine* e, int32_t launches[4], double mean_ms[4], cudaStream_t st) {
   if (e->ckpt_k) return fail(SWIT_E_STATE, "this call needs boundary saving (checkpoint_every = 0)");
-  if (e->variant == 3 && e->path == 0) return profile_vec_groups<R>(e, launches, mean_ms, st);
+  if (e->variant == 3 && e->path == 0) return profile_vec_graphs<R>(e, launches, mean_ms, st);
   Grid<R> g = make_grid<R>(e);
   const int nshot_launch = e->path == 1 ? 1 : e->batch;
   std::vector<cudaEvent_t> ev[4];
@@ -2249,6 +2235,49 @@ int swit_import_snapshot(swit_engine* e, const float* src, const float* boundary
   cudaStream_t st = (cudaStream_t)stream;
   return e->prec ? import_impl<double>(e, src, boundary, p_end, u_end, w_end, on_device, st)
                  : import_impl<float>(e, src, boundary, p_end, u_end, w_end, on_device, st);
+}
+
+namespace {
+// Read-modify-write sweeps over a buffer, loads and stores through L2 only
+// (ld.global.cg / st.global.cg): every thread touches the same 16-byte words on
+// every sweep, so a buffer that fits the L2 is served from it.
+__global__ void k_l2_rmw(float4* __restrict__ a, size_t n, int reps) {
+  for (int r = 0; r < reps; ++r)
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+      float4 v = __ldcg(a + i);
+      v.x += 1.f;
+      __stcg(a + i, v);
+    }
+}
+}  // namespace
+
+int swit_l2_bandwidth(int64_t bytes, int32_t reps, double* gbs, void* stream) {
+  if (!gbs || bytes < (1 << 20) || reps < 1) return fail(SWIT_E_ARG, "bytes >= 1 MiB, reps >= 1 and gbs required");
+  cudaStream_t st = (cudaStream_t)stream;
+  int dev = 0, sms = 0;
+  CK(cudaGetDevice(&dev));
+  CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  const size_t n = (size_t)bytes / 16;
+  float4* a = nullptr;
+  CK(cudaMalloc(&a, n * 16));
+  cudaEvent_t t0 = nullptr, t1 = nullptr;
+  cudaEventCreate(&t0);
+  cudaEventCreate(&t1);
+  cudaMemsetAsync(a, 0, n * 16, st);
+  const int grid = sms * 8;
+  k_l2_rmw<<<grid, 256, 0, st>>>(a, n, 2);  // brings the buffer into the L2
+  cudaEventRecord(t0, st);
+  k_l2_rmw<<<grid, 256, 0, st>>>(a, n, reps);
+  cudaEventRecord(t1, st);
+  cudaError_t ce = cudaEventSynchronize(t1);
+  float ms = 0.f;
+  if (ce == cudaSuccess) ce = cudaEventElapsedTime(&ms, t0, t1);
+  cudaEventDestroy(t0);
+  cudaEventDestroy(t1);
+  cudaFree(a);
+  if (ce != cudaSuccess) return fail(SWIT_E_CUDA, "swit_l2_bandwidth: %s", cudaGetErrorString(ce));
+  *gbs = 2.0 * (double)n * 16 * reps / (ms * 1e-3) / 1e9;
+  return 0;
 }
 
 int swit_profile_kernels(swit_engine* e, int32_t launches[4], double mean_ms[4], void* stream) {

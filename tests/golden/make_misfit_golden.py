@@ -1,7 +1,7 @@
 """Generates tests/golden/misfit_golden.npz from the reference's own misfit code.
 
-Imports toolbox/misfit.py of the reference (path given on the command line,
-default /root/reference/toolbox) with a minimal stand-in for obspy, which the
+Imports toolbox/misfit.py of the reference (directory given on the command line
+or in SWIT_REFERENCE_TOOLBOX) with a minimal stand-in for obspy, which the
 reference imports at module level (toolbox/tools.py:19-21) but is not installed
 here: a trace list whose items carry ``.data`` and ``.stats.sampling_rate``,
 the only attributes misfit.py and tools.get_su_parameter / su2array read.
@@ -64,7 +64,9 @@ def inputs():
 
 
 def main():
-    toolbox = sys.argv[1] if len(sys.argv) > 1 else "/root/reference/toolbox"
+    toolbox = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("SWIT_REFERENCE_TOOLBOX")
+    if not toolbox:
+        sys.exit("usage: %s <reference toolbox directory> (or set SWIT_REFERENCE_TOOLBOX)" % sys.argv[0])
     _stub_obspy()
     sys.path.insert(0, toolbox)
     import misfit as M  # the reference's toolbox/misfit.py

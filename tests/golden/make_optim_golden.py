@@ -66,7 +66,9 @@ def run(mod, scheme, steps=(0.5, 0.5, 0.5, 0.5)):
 
 
 def main():
-    toolbox = sys.argv[1] if len(sys.argv) > 1 else "/root/reference/toolbox"
+    toolbox = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("SWIT_REFERENCE_TOOLBOX")
+    if not toolbox:
+        sys.exit("usage: %s <reference toolbox directory> (or set SWIT_REFERENCE_TOOLBOX)" % sys.argv[0])
     _stubs()
     sys.path.insert(0, toolbox)
     dst = os.path.join(os.path.dirname(os.path.abspath(__file__)), "optim_golden.npz")

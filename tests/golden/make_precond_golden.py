@@ -49,7 +49,9 @@ def cases():
 
 
 def main():
-    toolbox = sys.argv[1] if len(sys.argv) > 1 else "/root/reference/toolbox"
+    toolbox = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("SWIT_REFERENCE_TOOLBOX")
+    if not toolbox:
+        sys.exit("usage: %s <reference toolbox directory> (or set SWIT_REFERENCE_TOOLBOX)" % sys.argv[0])
     _stubs()
     sys.path.insert(0, toolbox)
     import postprocess as P  # the reference's toolbox/postprocess.py

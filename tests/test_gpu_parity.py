@@ -314,16 +314,17 @@ def test_checkpointed_gradient_l2_and_snapshot_refusal(base):
     assert r["misfit"] == r0["misfit"]
 
 
-@pytest.mark.parametrize("opts,groups", [(dict(kernel="vec", shots_per_batch=1, graph_branches=2), 2),
-                                         (dict(kernel="vec", shots_per_batch=1, graph_branches=3), 1),
-                                         (dict(kernel="vec", shots_per_batch=1, graph_branches=1), 3),
-                                         (dict(kernel="split"), 1)])
-def test_kernel_profile_counts_launches_and_leaves_results_intact(base, opts, groups):
-    """swit_profile_kernels times every step launch (vec: each group of batches
-    launched together on the graph's branches); the engine still computes the
-    oracle's gradient afterwards."""
+@pytest.mark.parametrize("opts,launches", [(dict(kernel="vec", shots_per_batch=1, graph_branches=2), 3 * 256),
+                                           (dict(kernel="vec", shots_per_batch=1, graph_branches=3), 3 * 256),
+                                           (dict(kernel="vec", shots_per_batch=2, graph_branches=1), 2 * 256),
+                                           (dict(kernel="split"), 299)])
+def test_kernel_profile_counts_launches_and_leaves_results_intact(base, opts, launches):
+    """swit_profile_kernels times the batched vec kernels each in a graph of
+    min(nt-1, 256) steps of every batch (the split kernels: every launch of a
+    forward and reverse loop, all shots per launch); the engine still computes the
+    oracle's results afterwards."""
     s = base["s"]
-    assert s.ns == 3
+    assert s.ns == 3 and s.nt == 300
     with engine(s, **opts) as e:
         e.set_model(s.vp_true, base["rho"])
         e.forward(base["src"], save_boundary=True)
@@ -331,8 +332,9 @@ def test_kernel_profile_counts_launches_and_leaves_results_intact(base, opts, gr
         prof = e.profile_kernels()
         seis = e.forward(base["src"], save_boundary=True)
         g, fw, bk = e.backward(base["adj"])
+    assert set(prof) == {"fwd_p", "fwd_uw", "bwd_uw", "bwd_p"}
     for k, v in prof.items():
-        assert v["launches"] == groups * (s.nt - 1), k
+        assert v["launches"] == launches, k
         assert v["mean_ms"] > 0, k
     np.testing.assert_array_equal(seis, base["ref"]["seis"])
     np.testing.assert_array_equal(g, base["grad"]["g"])
