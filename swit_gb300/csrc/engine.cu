@@ -78,6 +78,7 @@ struct swit_engine {
   std::vector<uint32_t> h_list;  // host copy of the four lists (multi-instance engines combine them)
   // band variant: columns per band, bands, per-band task lists and counts of the four kernels
   int band_bc = 0, nbands = 0, band_stride = 0;
+  unsigned band_wait = 0;  // mbarrier polls before a band block gives up (SWIT_BAND_WAIT_POLLS lowers it)
   uint32_t* d_blist = nullptr;
   int4* d_bcnt = nullptr;
   size_t band_sm[4] = {0, 0, 0, 0};
@@ -241,7 +242,7 @@ void launch_pdl(bool pdl, void (*k)(P...), dim3 grid, dim3 block, cudaStream_t s
 // Band variant: one block per band of e->band_bc columns and shot.
 inline BandList band_list(const swit_engine* e, int k) {
   return BandList{e->d_blist + (size_t)k * e->nbands * e->band_stride, e->d_bcnt + (size_t)k * e->nbands,
-                  e->band_stride, e->band_bc};
+                  e->band_stride, e->band_bc, e->band_wait};
 }
 
 // Vec kernels: 256 threads per block over the kernel's task list k, nb shots.
@@ -1572,6 +1573,8 @@ struct swit_multi {
     size_t boff[4] = {0, 0, 0, 0};
     std::vector<int> act[4];
     std::vector<int> rows;         // table rows with a pair in this wave
+    // a wave of one instance runs that instance's own vec kernels on its shots [s0, s0 + nb)
+    int s0 = 0, nb = 0;
     cudaGraphExec_t g[3] = {nullptr, nullptr, nullptr};  // its forward (no strips, strips) and reverse loops
   };
   std::vector<Wave> waves;
@@ -1700,6 +1703,10 @@ int multi_build(swit_multi* m) {
     w.max_nt = m->eng[m->order[gr.front().first]]->nt;
     for (auto& pr : gr)
       if (w.rows.empty() || w.rows.back() != pr.first) w.rows.push_back(pr.first);
+    if (w.rows.size() == 1) {  // the pairs of one instance are consecutive shots
+      w.s0 = gr.front().second;
+      w.nb = (int)gr.size();
+    }
     for (int k = 0; k < 4; ++k) {
       w.boff[k] = B[k].size();
       std::vector<int> cum;  // blocks up to and including each pair
@@ -1762,7 +1769,15 @@ int multi_loop(swit_multi* m, int which, const std::vector<int>& on, cudaStream_
     cudaError_t rc = cudaStreamBeginCapture(m->cap, cudaStreamCaptureModeThreadLocal);
     if (rc != cudaSuccess) return fail(SWIT_E_CUDA, "multi-instance graph capture: %s", cudaGetErrorString(rc));
     auto ml = [&](int k, int nb) { return MultiLaunch{m->d_blocks[k] + w.boff[k], m->d_list[k], m->d_on, nb}; };
-    if (which < 2) {
+    if (w.rows.size() == 1) {
+      // one instance: its own single-instance kernels (same bodies, same bits), without
+      // the instance table or the per-instance block padding of the shared kernels
+      swit_engine* e = m->eng[m->order[w.rows[0]]];
+      if (which < 2)
+        launch_forward_steps<float>(e, which == 1, w.s0, w.nb, m->cap);
+      else
+        launch_backward_steps<float>(e, w.s0, w.nb, m->cap);
+    } else if (which < 2) {
       for (int it = 2; it <= w.max_nt; ++it) {
         launch_pdl(true, k_fwd_p_m<float>, grid(w.act[0][it]), block, m->cap, tab, ml(0, w.act[0][it]), it);
         launch_pdl(true, k_fwd_uw_m<float>, grid(w.act[1][it]), block, m->cap, tab, ml(1, w.act[1][it]), it,
@@ -1943,6 +1958,11 @@ int swit_create(const swit_desc* d, swit_engine** out) {
   }
   e->branches = d->graph_branches ? d->graph_branches : 2;
   e->graph_nodes = kGraphNodes;
+  e->band_wait = kBandWaitLimit;
+  if (const char* bw = std::getenv("SWIT_BAND_WAIT_POLLS")) {  // a shorter wait, e.g. to test the timeout path
+    const long long v = std::atoll(bw);
+    if (v >= 0 && v < (long long)kBandWaitLimit) e->band_wait = (unsigned)v;
+  }
   if (const char* gn = std::getenv("SWIT_GRAPH_NODES")) {  // smaller graphs, e.g. to test the chunking
     const long long v = std::atoll(gn);
     if (v > 0) e->graph_nodes = (size_t)v;

@@ -28,7 +28,8 @@ struct BandList {
   const uint32_t* __restrict__ e;
   const int4* __restrict__ cnt;
   int stride;
-  int bc;  // columns per band
+  int bc;         // columns per band
+  unsigned wait;  // polls of the mbarrier before a block gives up (kBandWaitLimit unless set lower)
 };
 
 constexpr unsigned kBandWaitLimit = 1u << 22;  // polls of the mbarrier before a block gives up
@@ -46,10 +47,10 @@ __device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
                : "memory");
 }
 
-// Bounded wait for phase `parity` of the mbarrier; false on timeout.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned parity) {
+// Bounded wait for phase `parity` of the mbarrier: at most `limit` polls; false on timeout.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned parity, unsigned limit = kBandWaitLimit) {
   const uint32_t a = smem_addr(bar);
-  for (unsigned n = 0; n < kBandWaitLimit; ++n) {
+  for (unsigned n = 0; n < limit; ++n) {
     uint32_t done;
     asm volatile(
         "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
@@ -115,10 +116,12 @@ __device__ __forceinline__ void band_task(const Grid<R>& g, const BandList& L, c
   t = i < cnt.x ? 0 : (i < cnt.y ? 1 : 2);
 }
 
-// Waits for the staged copies; on timeout every thread of the block learns it,
-// thread 0 records it and waits once more (bounded) for the copies in flight.
-__device__ __forceinline__ bool band_ready(uint64_t* bar, int* err) {
-  const bool ok = mbar_wait(bar, 0);
+// Waits (at most `limit` polls) for the staged copies; on timeout every thread
+// of the block learns it, thread 0 records it and waits once more, with the full
+// bound, for the copies in flight, so the block never leaves with a copy still
+// writing its shared memory.
+__device__ __forceinline__ bool band_ready(uint64_t* bar, int* err, unsigned limit) {
+  const bool ok = mbar_wait(bar, 0, limit);
   const bool bad = __syncthreads_or(!ok);
   if (bad && threadIdx.x == 0) {
     atomicOr(err, kErrBandTimeout);
@@ -171,7 +174,7 @@ __global__ void __launch_bounds__(256, SWIT_BAND_BLOCKS)
     BAND_LOAD(sk, 0, g.kp, b.c0, b.ncol);
   }
   const int4 cnt = L.cnt[blockIdx.x];
-  if (!band_ready(&bar, err)) return;
+  if (!band_ready(&bar, err, L.wait)) return;
   Grid<R> gl = g;
   gl.A = sa - 2 * LD;
   gl.kp = sk - 2 * LD;
@@ -218,7 +221,7 @@ __global__ void __launch_bounds__(256, SWIT_BAND_BLOCKS)
     BAND_LOAD(skw, 0, g.kw, b.c0, b.ncol);
   }
   const int4 cnt = L.cnt[blockIdx.x];
-  if (!band_ready(&bar, err)) return;
+  if (!band_ready(&bar, err, L.wait)) return;
   Grid<R> gl = g;
   gl.B = sb - 2 * LD;
   gl.ku = sku - 2 * LD;
@@ -279,7 +282,7 @@ __global__ void __launch_bounds__(256, SWIT_BAND_BLOCKS)
     BAND_LOAD(skw, 0, g.kw, b.c0, b.ncol);
   }
   const int4 cnt = L.cnt[blockIdx.x];
-  if (!band_ready(&bar, err)) return;
+  if (!band_ready(&bar, err, L.wait)) return;
   Grid<R> gl = g;
   gl.A = sa - 2 * LD;
   gl.B = sb - 2 * LD;
@@ -351,7 +354,7 @@ __global__ void __launch_bounds__(256, SWIT_BAND_BLOCKS)
     BAND_LOAD(sd, 0, DBK + off, b.c0, b.ncol);
   }
   const int4 cnt = L.cnt[blockIdx.x];
-  if (!band_ready(&bar, err)) return;
+  if (!band_ready(&bar, err, L.wait)) return;
   Grid<R> gl = g;
   gl.A = sa - 2 * LD;
   gl.B = sb - 2 * LD;

@@ -499,3 +499,26 @@ def test_walk_tiles_narrower_than_the_halo_and_tall_columns(block_x, nz, npml):
     np.testing.assert_array_equal(g, gref["g"])
     np.testing.assert_array_equal(fw, gref["fw"])
     np.testing.assert_array_equal(bk, gref["bk"])
+
+
+def test_band_wait_timeout_is_reported_and_the_context_stays_usable(base, monkeypatch):
+    """The band kernels' bounded mbarrier wait made to run out: with a poll
+    limit of 0 (SWIT_BAND_WAIT_POLLS) every block gives up at once, records
+    SWIT_E_TIMEOUT in the engine's error word, waits with the full bound for its
+    own copies in flight and leaves without updating.  check() raises and clears
+    the word; nothing faults or hangs, and an engine created afterwards on the
+    same context computes the oracle's seismograms."""
+    s = base["s"]
+    monkeypatch.setenv("SWIT_BAND_WAIT_POLLS", "0")
+    with engine(s, kernel="band") as e:
+        e.set_model(s.vp_true, base["rho"])
+        e.forward(base["src"], save_boundary=True)
+        with pytest.raises(SwitError, match="SWIT_E_TIMEOUT"):
+            e.check()
+        e.check()  # the word was cleared
+    monkeypatch.delenv("SWIT_BAND_WAIT_POLLS")
+    with engine(s, kernel="band") as e:
+        e.set_model(s.vp_true, base["rho"])
+        seis = e.forward(base["src"], save_boundary=True)
+        e.check()
+    np.testing.assert_array_equal(seis, base["ref"]["seis"])
