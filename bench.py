@@ -49,14 +49,17 @@ def parse():
     ap.add_argument("--kernel", default="auto", choices=["auto", "walk", "split", "vec", "cluster", "hybrid", "band"])
     ap.add_argument("--no-tune", action="store_true", help="skip the launch-configuration autotuner")
     ap.add_argument("--no-extras", action="store_true", help="skip plain path, CPU baseline and kernel profile")
-    ap.add_argument("--workload", default="marmousi", choices=["marmousi", "large", "multi", "correlation"],
-                    help="marmousi: 481x141 nt 4000 49 shots (the headline); large: 2001x601 nt 6000 200 shots; "
+    ap.add_argument("--workload", default="marmousi", choices=["marmousi", "small", "large", "multi", "correlation"],
+                    help="marmousi: 481x141 nt 4000 49 shots (the headline); small: 201x101 nt 2000 5 shots; "
+                         "large: 2001x601 nt 6000 200 shots; "
                          "multi: uneven independent FWI problems, L-BFGS on all at once vs one after another; "
                          "correlation: 501x171 nt 5000 51 shots, global-correlation + traveltime misfits "
                          "through torch.autograd")
     ap.add_argument("--instances", type=int, default=64, help="multi: problems")
     ap.add_argument("--iters", type=int, default=5, help="multi: L-BFGS iterations")
     ap.add_argument("--scale", type=float, default=1.0, help="multi: factor on shot counts and record lengths")
+    ap.add_argument("--parity-shots", type=int, default=16,
+                    help="large: shots of the full-size comparison with the FP64 build and the oracle (0: none)")
     ap.add_argument("--plain-lbfgs", action="store_true",
                     help="multi: run the plain path's L-BFGS in full (default: one plain gradient of every problem)")
     ap.add_argument("--checkpoint", default="0",
@@ -239,6 +242,29 @@ def full_size_parity(sv, rho, src_d, obs_d, mine, ref32=None):
     return out
 
 
+def subset_parity(sv, rho, n):
+    """The full-size comparison on n of the workload's shots, evenly spread
+    (full grid and nt): FP32 engine against the FP64 build and the FP32 oracle."""
+    import dataclasses
+
+    import torch
+
+    from swit_gb300 import Engine
+    keep = np.linspace(0, sv.ns - 1, min(n, sv.ns)).round().astype(int)
+    sub = dataclasses.replace(sv, src_xz=sv.src_xz[keep].copy(), rec_xz=sv.rec_xz[keep].copy())
+    src_d = torch.from_numpy(sub.source()).cuda()
+    with Engine(**sub.engine_args()) as e:
+        e.set_model(sub.vp_true, rho)
+        obs_d = e.forward(src_d, save_boundary=False)
+        e.set_model(sub.vp_init, rho)
+        mine = e.gradient_l2(src_d, obs_d, return_seis=True)
+    ref32, wall = oracle_gradient(sub, rho, sub.source(), obs_d.cpu().numpy(), os.cpu_count() or 1)
+    out = full_size_parity(sub, rho, src_d, obs_d, mine, ref32)
+    out["shot_indices"] = [int(k) for k in keep]
+    out["oracle_wall_s"] = wall
+    return out
+
+
 def cpu_with_strip_io(sv, rho, src, obs, threads):
     """The same sample as cpu_baseline, but with fd2dmpi's file round trip: the
     forward job writes each shot's boundary strips and final wavefields to files
@@ -286,10 +312,13 @@ def cpu_with_strip_io(sv, rho, src, obs, threads):
 
 def workload_config(sv, shots):
     """The workload as both arms name it (identical keys and values)."""
+    strips = shots * sv.nt * (9 * sv.nx + 6 * sv.nz) * 4
+    traces = 2 * shots * sv.ng * sv.nt * 4
+    l2 = ("inputs larger than L2" if strips + traces > 126e6 else "inputs smaller than L2, no flush between steps")
     return {"workload": sv.name, "grid": [sv.nx, sv.nz], "npml": sv.npml, "nt": sv.nt, "shots_per_gpu": shots,
             "receivers": sv.ng, "dx_m": sv.dx, "dt_s": sv.dt,
-            "l2": "inputs larger than L2: each step streams %.2f GB of boundary strips and %.2f GB of traces"
-                  % (shots * sv.nt * (9 * sv.nx + 6 * sv.nz) * 4 / 1e9, 2 * shots * sv.ng * sv.nt * 4 / 1e9)}
+            "l2": "%s: each step streams %.2f GB of boundary strips and %.2f GB of traces"
+                  % (l2, strips / 1e9, traces / 1e9)}
 
 
 def run_reference(args):
@@ -351,8 +380,9 @@ def run_mine(args):
     exact = args.adjoint == "exact"
     if exact:  # the kernel profile, plain path and CPU baseline time fd2dmpi's adjoint
         args.no_extras = True
-    per_rank = args.shots or (200 if large else 49)
-    full = survey.config(3 if large else 1, ns=per_rank * world, nt=args.nt)
+    small = args.workload == "small"
+    per_rank = args.shots or (200 if large else (5 if small else 49))
+    full = survey.config(3 if large else (0 if small else 1), ns=per_rank * world, nt=args.nt)
     # rank r owns a contiguous block of shots (fd2dmpi/mmi_mpi.f90:52-80)
     lo, hi = shots.assigned(per_rank * world, rank, world)
     sv = full
@@ -536,6 +566,8 @@ def run_mine(args):
             line["parity"] = full_size_parity(sv, rho, src_d, obs_d, fin, ref32)
             del ref32, fin
     eng.close()
+    if large and rank == 0 and world == 1 and args.parity_shots > 0:
+        line["parity"] = subset_parity(sv, rho, args.parity_shots)
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:
@@ -746,6 +778,17 @@ def run_correlation(args):
                     "d2h_bytes_per_step": int(sv.nx * sv.nz * 4 + 4)},
             "clocks": clk,
             "gpu_launches": int(args.steps * (q["kernels_per_forward"] + q["kernels_per_backward"] + 5))}
+    if not args.no_extras and args.adjoint == "fd2dmpi":
+        # the engine's Waveform gradient of every shot at this size against the FP64 build and the oracle
+        rho_h = sv.rho(sv.vp_true)
+        eng.set_model(vp0, rho)
+        mine = eng.gradient_l2(src, obs, return_seis=True)
+        ref32, wall = oracle_gradient(sv, rho_h, sv.source(), obs.cpu().numpy(), os.cpu_count() or 1)
+        line["parity"] = full_size_parity(sv, rho_h, src, obs, mine, ref32)
+        line["parity"]["misfit"] = "Waveform (the correlation misfits' gradients run the same reverse loop)"
+        line["cpu_baseline"] = {"value": sv.ns / wall, "unit": "shot-gradients/s", "cores": os.cpu_count() or 1,
+                                "kind": "port", "sample": "Waveform gradient of all %d shots at full nt=%d, one shot "
+                                                          "per thread, %.1f s wall" % (sv.ns, sv.nt, wall)}
     print(json.dumps(line), flush=True)
 
 
