@@ -114,6 +114,11 @@ struct swit_engine {
   // further capture streams: batches run round-robin over the branches of the graphs (capture_fork)
   cudaStream_t capx[kCapStreamsMax - 1] = {};
   cudaEvent_t ev_fork = nullptr, ev_join[kCapStreamsMax - 1] = {};
+  // host observed data of swit_gradient_l2: copied into d_in on `cpy` while the
+  // forward loop runs (ev_in: the call's start on the caller's stream; ev_cpy: copy done)
+  cudaStream_t cpy = nullptr;
+  cudaEvent_t ev_in = nullptr, ev_cpy = nullptr;
+  float* d_src_in = nullptr;  // source staging (ns x nt floats), apart from d_in
   int branches = 2;  // graph branches in use (swit_desc.graph_branches)
   // captured loops, each a sequence of graphs of at most kGraphNodes nodes (capture_chunked)
   std::vector<cudaGraphExec_t> gfwd[2];
@@ -164,9 +169,12 @@ void release(swit_engine* e) {
     if (e->ev_join[i]) cudaEventDestroy(e->ev_join[i]);
   }
   if (e->ev_fork) cudaEventDestroy(e->ev_fork);
+  if (e->cpy) cudaStreamDestroy(e->cpy);
+  if (e->ev_in) cudaEventDestroy(e->ev_in);
+  if (e->ev_cpy) cudaEventDestroy(e->ev_cpy);
   void* ptrs[] = {e->d_rcol, e->d_zlo, e->d_zhi, e->d_ng, e->d_isx, e->d_isz, e->d_risx, e->d_risz, e->d_colptr, e->d_ig, e->d_zr, e->d_live,
                   e->d_mtrace, e->A, e->B, e->damp, e->cint, e->kp, e->ku, e->kw, e->p, e->u, e->w, e->pb, e->ub, e->wb, e->pe,
-                  e->ue, e->we, e->dg, e->dfw, e->dbk, e->strips, e->src, e->seis_t, e->adj_t, e->d_in,
+                  e->ue, e->we, e->dg, e->dfw, e->dbk, e->strips, e->src, e->seis_t, e->adj_t, e->d_in, e->d_src_in,
                   e->d_stage, e->p2, e->u2, e->w2, e->pb2, e->ub2, e->wb2, e->pe2, e->ue2, e->we2, e->d_list, e->d_blist, e->d_bcnt, e->d_err, e->ckpt,
                   e->xm, e->xsrc, e->xdadc};
   for (void* q : ptrs)
@@ -767,9 +775,11 @@ template <class R>
 int forward_impl(swit_engine* e, const float* src, void* seis, bool store, int on_device, cudaStream_t st,
                  bool run_loop = true) {
   Grid<R> g = make_grid<R>(e);
-  const float* dsrc;
-  int rc = stage_input(e, src, (size_t)e->ns * e->nt, on_device, st, &dsrc);
-  if (rc) return rc;
+  const float* dsrc = src;
+  if (!on_device) {
+    CK(cudaMemcpyAsync(e->d_src_in, src, (size_t)e->ns * e->nt * sizeof(float), cudaMemcpyHostToDevice, st));
+    dsrc = e->d_src_in;
+  }
   k_src_in<R><<<nblocks((size_t)e->ns * (e->nt + 1)), 256, 0, st>>>(dsrc, (R*)e->src, e->ns, e->nt);
   const size_t fb = (size_t)e->ns * g.FSZ * e->esz;
   CK(cudaMemsetAsync(e->p, 0, fb, st));
@@ -781,7 +791,7 @@ int forward_impl(swit_engine* e, const float* src, void* seis, bool store, int o
     CK(cudaMemsetAsync(e->w2, 0, fb, st));
   }
   if (run_loop) {  // a multi-instance engine runs the loops of all its instances itself
-    rc = run_forward_loop<R>(e, store, st);
+    const int rc = run_forward_loop<R>(e, store, st);
     if (rc) return rc;
   }
   if (seis) {
@@ -966,10 +976,25 @@ int misfit_sum(swit_engine* e, cudaStream_t st, double* misfit) {
 template <class R>
 int gradient_impl(swit_engine* e, const float* src, const float* obs, void* grad, void* fw, void* bk, void* seis,
                   double* misfit, int on_device, cudaStream_t st) {
-  // the forward stages the source through d_in; obs needs its own staging
+  // Host observed data: copied into d_in on the engine's copy stream while the
+  // forward loop runs (the copy waits for everything queued on st before this
+  // call, e.g. the previous call's residual reading d_in), and the residual
+  // waits for the copy.
+  const float* dobs = obs;
+  if (!on_device) {
+    CK(cudaEventRecord(e->ev_in, st));
+    CK(cudaStreamWaitEvent(e->cpy, e->ev_in, 0));
+  }
   int rc = forward_impl<R>(e, src, seis, true, on_device, st);
   if (rc) return rc;
-  rc = residual_l2<R>(e, obs, on_device, st);
+  if (!on_device) {
+    CK(cudaMemcpyAsync(e->d_in, obs, (size_t)e->ns * e->ngmax * e->nt * sizeof(float), cudaMemcpyHostToDevice,
+                       e->cpy));
+    CK(cudaEventRecord(e->ev_cpy, e->cpy));
+    CK(cudaStreamWaitEvent(st, e->ev_cpy, 0));
+    dobs = e->d_in;
+  }
+  rc = residual_l2<R>(e, dobs, 1, st);
   if (rc) return rc;
   rc = e->exact ? exact_core<R>(e, grad, nullptr, on_device, st) : backward_core<R>(e, grad, fw, bk, on_device, st);
   if (rc) return rc;
@@ -2105,6 +2130,7 @@ int swit_create(const swit_desc* d, swit_engine** out) {
   AL(valloc(e, &e->seis_t, (size_t)ns * e->nt * ngm));
   AL(valloc(e, &e->adj_t, (size_t)ns * e->nt * ngm));
   AL(dalloc(e, &e->d_in, (size_t)ns * ngm * e->nt));
+  AL(dalloc(e, &e->d_src_in, (size_t)ns * e->nt));
   AL(valloc(e, &e->d_stage, std::max((size_t)ns * ngm * e->nt, (size_t)3 * nx * nz)));
 #undef AL
   auto h2d = [&](void* dst, const void* src, size_t bytes) -> int {
@@ -2153,6 +2179,9 @@ int swit_create(const swit_desc* d, swit_engine** out) {
     if (ce == cudaSuccess) ce = cudaEventCreateWithFlags(&e->ev_join[i], cudaEventDisableTiming);
   }
   if (ce == cudaSuccess) ce = cudaEventCreateWithFlags(&e->ev_fork, cudaEventDisableTiming);
+  if (ce == cudaSuccess) ce = cudaStreamCreateWithFlags(&e->cpy, cudaStreamNonBlocking);
+  if (ce == cudaSuccess) ce = cudaEventCreateWithFlags(&e->ev_in, cudaEventDisableTiming);
+  if (ce == cudaSuccess) ce = cudaEventCreateWithFlags(&e->ev_cpy, cudaEventDisableTiming);
   if (ce != cudaSuccess) {
     rc = fail(SWIT_E_CUDA, "engine initialisation: %s", cudaGetErrorString(ce));
     release(e);
