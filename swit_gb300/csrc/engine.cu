@@ -75,6 +75,12 @@ struct swit_engine {
   uint32_t* d_list = nullptr;
   size_t list_stride = 0;
   int list_n0[4] = {0, 0, 0, 0}, list_n1[4] = {0, 0, 0, 0}, list_len[4] = {0, 0, 0, 0};
+  // the device lists of the single-instance kernels: the full lists above minus
+  // the tier-0 rectangle of each kernel, whose vectors the first rect_nb blocks
+  // map arithmetically (VecList); the multi-instance engine uses the full lists
+  int dl_n0[4] = {0, 0, 0, 0}, dl_n1[4] = {0, 0, 0, 0}, dl_len[4] = {0, 0, 0, 0};
+  int rect_x0[4] = {0, 0, 0, 0}, rect_q0[4] = {0, 0, 0, 0}, rect_nq[4] = {1, 1, 1, 1}, rect_n[4] = {0, 0, 0, 0};
+  uint32_t* d_dlist = nullptr;
   std::vector<uint32_t> h_list;  // host copy of the four lists (multi-instance engines combine them)
   // band variant: columns per band, bands, per-band task lists and counts of the four kernels
   int band_bc = 0, nbands = 0, band_stride = 0;
@@ -175,7 +181,7 @@ void release(swit_engine* e) {
   void* ptrs[] = {e->d_rcol, e->d_zlo, e->d_zhi, e->d_ng, e->d_isx, e->d_isz, e->d_risx, e->d_risz, e->d_colptr, e->d_ig, e->d_zr, e->d_live,
                   e->d_mtrace, e->A, e->B, e->damp, e->cint, e->kp, e->ku, e->kw, e->p, e->u, e->w, e->pb, e->ub, e->wb, e->pe,
                   e->ue, e->we, e->dg, e->dfw, e->dbk, e->strips, e->src, e->seis_t, e->adj_t, e->d_in, e->d_src_in,
-                  e->d_stage, e->p2, e->u2, e->w2, e->pb2, e->ub2, e->wb2, e->pe2, e->ue2, e->we2, e->d_list, e->d_blist, e->d_bcnt, e->d_err, e->ckpt,
+                  e->d_stage, e->p2, e->u2, e->w2, e->pb2, e->ub2, e->wb2, e->pe2, e->ue2, e->we2, e->d_list, e->d_dlist, e->d_blist, e->d_bcnt, e->d_err, e->ckpt,
                   e->xm, e->xsrc, e->xdadc};
   for (void* q : ptrs)
     if (q) cudaFree(q);
@@ -255,11 +261,12 @@ inline BandList band_list(const swit_engine* e, int k) {
 
 // Vec kernels: 256 threads per block over the kernel's task list k, nb shots.
 inline VecList vec_list(const swit_engine* e, int k) {
-  return VecList{e->d_list + (size_t)k * e->list_stride, e->list_n0[k], e->list_n1[k], e->list_len[k]};
+  return VecList{e->d_dlist + (size_t)k * e->list_stride, e->dl_n0[k], e->dl_n1[k], e->dl_len[k], e->rect_x0[k],
+                 e->rect_q0[k], e->rect_nq[k], e->rect_n[k], (e->rect_n[k] + 255) / 256};
 }
 inline dim3 vec_block(const swit_engine*) { return dim3(256); }
 inline dim3 vec_grid(const swit_engine* e, int k, int nb) {
-  return dim3((unsigned)std::max(1, (e->list_len[k] + 255) / 256), nb);
+  return dim3((unsigned)std::max(1, (e->rect_n[k] + 255) / 256 + (e->dl_len[k] + 255) / 256), nb);
 }
 
 // Cluster variant: one launch runs the whole time loop of nb shots, one
@@ -1426,6 +1433,44 @@ int build_lists(swit_engine* e) {
   int rc = dalloc(e, &e->d_list, 4 * n);
   if (rc) return rc;
   CK(cudaMemcpy(e->d_list, L.data(), 4 * n * sizeof(uint32_t), cudaMemcpyHostToDevice));
+  // Tier-0 rectangle of each kernel: the deep interior (columns [L+3, NX-L-3],
+  // vectors wholly in rows [L+4, NZ-L-3]; vec_flags), when every vector in it
+  // has tier 0 for that kernel (a deep source or receiver makes a hole: no
+  // rectangle then).  Its vectors leave the device list.
+  const int L0 = e->L, NZ = e->NZ;
+  const int xa = L0 + 2, xb = NX - L0 - 4;       // 0-based columns
+  const int qa = (L0 + 3 + 3) / 4, qb = (NZ - L0 - 7) / 4;  // 4q+1 >= L+4, 4q+4 <= NZ-L-3
+  bool use_rect = xb >= xa && qb >= qa;
+  if (const char* rv = std::getenv("SWIT_VEC_RECT")) use_rect = use_rect && std::atoi(rv) != 0;
+  std::vector<uint32_t> D(4 * n, 0u);
+  for (int k = 0; k < 4; ++k) {
+    const int* tk = &t[k * n];
+    bool ok = use_rect;
+    for (int x = xa; ok && x <= xb; ++x)
+      for (int q = qa; q <= qb; ++q)
+        if (tk[(size_t)x * LD4 + q] != 0) {
+          ok = false;
+          break;
+        }
+    const uint32_t* src = &L[k * n];
+    uint32_t* dst = &D[k * n];
+    int m = 0;
+    for (int i = 0; i < e->list_len[k]; ++i) {
+      const int x = (int)(src[i] >> 16), q = (int)(src[i] & 0xffffu);
+      if (ok && x >= xa && x <= xb && q >= qa && q <= qb) continue;
+      dst[m++] = src[i];
+    }
+    const int rn = ok ? (xb - xa + 1) * (qb - qa + 1) : 0;
+    e->rect_x0[k] = xa;
+    e->rect_q0[k] = qa;
+    e->rect_nq[k] = qb - qa + 1 > 0 ? qb - qa + 1 : 1;
+    e->rect_n[k] = rn;
+    e->dl_n0[k] = e->list_n0[k] - rn;  // the rectangle's vectors are tier-0 entries
+    e->dl_n1[k] = e->list_n1[k] - rn;
+    e->dl_len[k] = m;
+  }
+  if ((rc = dalloc(e, &e->d_dlist, 4 * n))) return rc;
+  CK(cudaMemcpy(e->d_dlist, D.data(), 4 * n * sizeof(uint32_t), cudaMemcpyHostToDevice));
   return 0;
 }
 

@@ -108,15 +108,34 @@ __device__ __forceinline__ void pdl_enter() {
 struct VecList {
   const uint32_t* __restrict__ e;
   int n0, n1, len;
+  // A rectangle of tier-0 vectors kept out of the list: columns [rx0+1, ...),
+  // rnq vectors from rq0 in each, rn vectors in all, covered by the first rnb
+  // blocks, whose threads find their vector arithmetically (no list load).
+  int rx0, rq0, rnq, rn, rnb;
 };
 
 // Thread -> (shot, vector, tier) from the list; false past its end.
 template <class R>
 __device__ __forceinline__ bool list_index(const Grid<R>& g, const VecList& L, int shot0, VecIdx& v, int& t) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= L.len) return false;
-  const uint32_t e = L.e[i];
   v.s = shot0 + blockIdx.y;
+  if ((int)blockIdx.x < L.rnb) {  // the tier-0 rectangle, column by column (uniform over the block)
+    const int r = (int)blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= L.rn) return false;
+    const int c = r / L.rnq;
+    v.ix = L.rx0 + c + 1;
+    v.q = L.rq0 + (r - c * L.rnq);
+    v.iz0 = 4 * v.q + 1;
+    v.ok = true;
+    v.k4 = (size_t)(v.ix - 1) * (g.LD >> 2) + v.q;
+    v.kc = v.k4;
+    v.kg = v.k4;
+    t = 0;
+    return true;
+  }
+  const int il = i - L.rnb * (int)blockDim.x;
+  if (il >= L.len) return false;
+  const uint32_t e = L.e[il];
   v.ix = (int)(e >> 16) + 1;
   v.q = (int)(e & 0xffffu);
   v.iz0 = 4 * v.q + 1;
@@ -124,7 +143,7 @@ __device__ __forceinline__ bool list_index(const Grid<R>& g, const VecList& L, i
   v.k4 = (size_t)(v.ix - 1) * (g.LD >> 2) + v.q;
   v.kc = v.k4;
   v.kg = v.k4;
-  t = i < L.n0 ? 0 : (i < L.n1 ? 1 : 2);
+  t = il < L.n0 ? 0 : (il < L.n1 ? 1 : 2);
   return true;
 }
 

@@ -522,3 +522,28 @@ def test_band_wait_timeout_is_reported_and_the_context_stays_usable(base, monkey
         seis = e.forward(base["src"], save_boundary=True)
         e.check()
     np.testing.assert_array_equal(seis, base["ref"]["seis"])
+
+
+@pytest.mark.parametrize("opts", [dict(), dict(adjoint="exact")])
+def test_tier0_rectangle_without_list_gives_the_same_bits(opts, monkeypatch):
+    """The vec kernels map the deep-interior tier-0 rectangle arithmetically and
+    take only the rest from their task lists; an engine with the rectangle
+    switched off (SWIT_VEC_RECT=0: everything from the lists) computes the same
+    bits, for fd2dmpi's adjoint and the exact adjoint."""
+    s = survey.small(nx=60, nz=44, npml=10, nt=180, ns=3)
+    src = s.source()
+    rho = s.rho(s.vp_true)
+    outs = []
+    for flag in ("1", "0"):
+        monkeypatch.setenv("SWIT_VEC_RECT", flag)
+        with Engine(**s.engine_args(), kernel="vec", **opts) as e:
+            e.set_model(s.vp_true, rho)
+            seis = e.forward(src, save_boundary=True)
+            adj = (seis * 0.25).astype(np.float32)
+            if opts.get("adjoint") == "exact":
+                g = e.backward_exact(adj)[0]
+            else:
+                g = e.backward(adj)[0]
+        outs.append((seis, g))
+    np.testing.assert_array_equal(outs[0][0], outs[1][0])
+    np.testing.assert_array_equal(outs[0][1], outs[1][1])
