@@ -262,11 +262,12 @@ inline BandList band_list(const swit_engine* e, int k) {
 // Vec kernels: 256 threads per block over the kernel's task list k, nb shots.
 inline VecList vec_list(const swit_engine* e, int k) {
   return VecList{e->d_dlist + (size_t)k * e->list_stride, e->dl_n0[k], e->dl_n1[k], e->dl_len[k], e->rect_x0[k],
-                 e->rect_q0[k], e->rect_nq[k], e->rect_n[k], (e->rect_n[k] + 255) / 256};
+                 e->rect_q0[k], e->rect_nq[k], e->rect_n[k], (e->rect_n[k] + SWIT_VEC_BLOCK - 1) / SWIT_VEC_BLOCK};
 }
-inline dim3 vec_block(const swit_engine*) { return dim3(256); }
+inline dim3 vec_block(const swit_engine*) { return dim3(SWIT_VEC_BLOCK); }
 inline dim3 vec_grid(const swit_engine* e, int k, int nb) {
-  return dim3((unsigned)std::max(1, (e->rect_n[k] + 255) / 256 + (e->dl_len[k] + 255) / 256), nb);
+  constexpr int B = SWIT_VEC_BLOCK;
+  return dim3((unsigned)std::max(1, (e->rect_n[k] + B - 1) / B + (e->dl_len[k] + B - 1) / B), nb);
 }
 
 // Cluster variant: one launch runs the whole time loop of nb shots, one

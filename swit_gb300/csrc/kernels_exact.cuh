@@ -36,7 +36,7 @@ namespace swit {
 // Forward pressure phase that also stores D of step it for the exact adjoint:
 // shot s, step it at dsave + (s * snt + it - sit0) * FSZ.
 template <class R>
-__global__ void __launch_bounds__(256, SWIT_VEC_MINB_R(R)) k_fwd_p_vx(Grid<R> g, VecList L, Sources src, const R* __restrict__ s_fwd, R* P,
+__global__ void __launch_bounds__(SWIT_VEC_BLOCK, SWIT_VEC_MINB_BLK(R)) k_fwd_p_vx(Grid<R> g, VecList L, Sources src, const R* __restrict__ s_fwd, R* P,
                                                   const R* __restrict__ U, const R* __restrict__ W, int it, int shot0,
                                                   R* __restrict__ dsave) {
   VecIdx v;
@@ -68,7 +68,7 @@ struct XAdj {
 };
 
 template <class R>
-__global__ void __launch_bounds__(256) k_xadj_p(Grid<R> g, VecList L, Receivers rec, Sources src, XAdj<R> x, int it,
+__global__ void __launch_bounds__(SWIT_VEC_BLOCK) k_xadj_p(Grid<R> g, VecList L, Receivers rec, Sources src, XAdj<R> x, int it,
                                                 int shot0) {
   VecIdx v;
   int t;
@@ -129,7 +129,7 @@ __global__ void __launch_bounds__(256) k_xadj_p(Grid<R> g, VecList L, Receivers 
 }
 
 template <class R>
-__global__ void __launch_bounds__(256, SWIT_VEC_MINB_R(R)) k_xadj_uw(Grid<R> g, VecList L, XAdj<R> x, int it, int shot0) {
+__global__ void __launch_bounds__(SWIT_VEC_BLOCK, SWIT_VEC_MINB_BLK(R)) k_xadj_uw(Grid<R> g, VecList L, XAdj<R> x, int it, int shot0) {
   VecIdx v;
   int t;
   const bool ok = list_index(g, L, shot0, v, t);

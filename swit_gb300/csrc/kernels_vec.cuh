@@ -89,6 +89,15 @@ __device__ __forceinline__ void vec_flags(const Grid<R>& g, VecIdx& v) {
 #define SWIT_VEC_MINB 4
 #endif
 #define SWIT_VEC_MINB_R(R) (sizeof(R) == 4 ? SWIT_VEC_MINB : 1)
+// Threads per block of the vec step kernels.  Measured at 481x141, 49 shots
+// (64 registers): 128 threads 133.6, 256: 127.3, 512: 118.9, 64: 119.0
+// shot-gradients/s -- 8 resident blocks per SM schedule and drain more finely.
+#ifndef SWIT_VEC_BLOCK
+#define SWIT_VEC_BLOCK 128
+#endif
+// Launch bounds of the vec step kernels: SWIT_VEC_BLOCK threads, registers
+// capped as for SWIT_VEC_MINB blocks of 256 threads per SM (FP32 builds)
+#define SWIT_VEC_MINB_BLK(R) (SWIT_VEC_MINB_R(R) * 256 / SWIT_VEC_BLOCK > 0 ? SWIT_VEC_MINB_R(R) * 256 / SWIT_VEC_BLOCK : 1)
 
 // Programmatic dependent launch: wait until the previous kernel in the stream
 // has completed and its writes are visible, then let the next kernel's blocks
@@ -318,7 +327,7 @@ __device__ __forceinline__ int tier_bwd_p(const Grid<R>& g, const VecIdx& v, boo
   } while (0)
 
 template <class R>
-__global__ void __launch_bounds__(256, SWIT_VEC_MINB_R(R)) k_fwd_p_v(Grid<R> g, VecList L, Sources src, const R* __restrict__ s_fwd, R* P,
+__global__ void __launch_bounds__(SWIT_VEC_BLOCK, SWIT_VEC_MINB_BLK(R)) k_fwd_p_v(Grid<R> g, VecList L, Sources src, const R* __restrict__ s_fwd, R* P,
                                                  const R* __restrict__ U, const R* __restrict__ W, int it, int shot0) {
   VecIdx v;
   int t;
@@ -440,7 +449,7 @@ __device__ __forceinline__ void fwd_uw_body(const Grid<R>& g, const Receivers& r
 }
 
 template <class R>
-__global__ void __launch_bounds__(256, SWIT_VEC_MINB_R(R)) k_fwd_uw_v(Grid<R> g, VecList L, Receivers rec, const R* __restrict__ P, R* U,
+__global__ void __launch_bounds__(SWIT_VEC_BLOCK, SWIT_VEC_MINB_BLK(R)) k_fwd_uw_v(Grid<R> g, VecList L, Receivers rec, const R* __restrict__ P, R* U,
                                                   R* W, R* __restrict__ seis_t, R* __restrict__ strips, int it,
                                                   int shot0) {
   VecIdx v;
@@ -554,7 +563,7 @@ __device__ __forceinline__ void bwd_uw_body(const Grid<R>& g, const R* __restric
 }
 
 template <class R>
-__global__ void __launch_bounds__(256, SWIT_VEC_MINB_R(R)) k_bwd_uw_v(Grid<R> g, VecList L, const R* __restrict__ PB, R* UB, R* WB,
+__global__ void __launch_bounds__(SWIT_VEC_BLOCK, SWIT_VEC_MINB_BLK(R)) k_bwd_uw_v(Grid<R> g, VecList L, const R* __restrict__ PB, R* UB, R* WB,
                                                   const R* __restrict__ PE, R* UE, R* WE,
                                                   const R* __restrict__ strips, int it, int shot0) {
   VecIdx v;
@@ -684,7 +693,7 @@ __device__ __forceinline__ void bwd_p_body(const Grid<R>& g, const Receivers& re
 
 // dg, dfw, dbk are the shot's imaging sums (indexed by v.kg).
 template <class R>
-__global__ void __launch_bounds__(256, SWIT_VEC_MINB_R(R)) k_bwd_p_v(Grid<R> g, VecList L, Receivers rec, Sources src,
+__global__ void __launch_bounds__(SWIT_VEC_BLOCK, SWIT_VEC_MINB_BLK(R)) k_bwd_p_v(Grid<R> g, VecList L, Receivers rec, Sources src,
                                                  const R* __restrict__ s_fwd, const R* __restrict__ adj_t, R* PB,
                                                  const R* __restrict__ UB, const R* __restrict__ WB, R* PE,
                                                  const R* __restrict__ UE, const R* __restrict__ WE, R* DG, R* DFW,
