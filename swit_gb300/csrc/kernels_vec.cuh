@@ -98,6 +98,17 @@ __device__ __forceinline__ void vec_flags(const Grid<R>& g, VecIdx& v) {
 // Launch bounds of the vec step kernels: SWIT_VEC_BLOCK threads, registers
 // capped as for SWIT_VEC_MINB blocks of 256 threads per SM (FP32 builds)
 #define SWIT_VEC_MINB_BLK(R) (SWIT_VEC_MINB_R(R) * 256 / SWIT_VEC_BLOCK > 0 ? SWIT_VEC_MINB_R(R) * 256 / SWIT_VEC_BLOCK : 1)
+// Own caps of the reverse velocity kernel, which fits 48 registers without
+// spilling (5: 134.7 vs 133.4 shot-gradients/s at 4), and of the forward
+// pressure kernel.
+#ifndef SWIT_VEC_MINB_BUW
+#define SWIT_VEC_MINB_BUW 5
+#endif
+#define SWIT_VEC_MINB_BUW_BLK(R) (sizeof(R) == 4 ? SWIT_VEC_MINB_BUW * 256 / SWIT_VEC_BLOCK : 1)
+#ifndef SWIT_VEC_MINB_FP
+#define SWIT_VEC_MINB_FP SWIT_VEC_MINB
+#endif
+#define SWIT_VEC_MINB_FP_BLK(R) (sizeof(R) == 4 ? SWIT_VEC_MINB_FP * 256 / SWIT_VEC_BLOCK : 1)
 
 // Programmatic dependent launch: wait until the previous kernel in the stream
 // has completed and its writes are visible, then let the next kernel's blocks
@@ -327,7 +338,7 @@ __device__ __forceinline__ int tier_bwd_p(const Grid<R>& g, const VecIdx& v, boo
   } while (0)
 
 template <class R>
-__global__ void __launch_bounds__(SWIT_VEC_BLOCK, SWIT_VEC_MINB_BLK(R)) k_fwd_p_v(Grid<R> g, VecList L, Sources src, const R* __restrict__ s_fwd, R* P,
+__global__ void __launch_bounds__(SWIT_VEC_BLOCK, SWIT_VEC_MINB_FP_BLK(R)) k_fwd_p_v(Grid<R> g, VecList L, Sources src, const R* __restrict__ s_fwd, R* P,
                                                  const R* __restrict__ U, const R* __restrict__ W, int it, int shot0) {
   VecIdx v;
   int t;
@@ -563,7 +574,7 @@ __device__ __forceinline__ void bwd_uw_body(const Grid<R>& g, const R* __restric
 }
 
 template <class R>
-__global__ void __launch_bounds__(SWIT_VEC_BLOCK, SWIT_VEC_MINB_BLK(R)) k_bwd_uw_v(Grid<R> g, VecList L, const R* __restrict__ PB, R* UB, R* WB,
+__global__ void __launch_bounds__(SWIT_VEC_BLOCK, SWIT_VEC_MINB_BUW_BLK(R)) k_bwd_uw_v(Grid<R> g, VecList L, const R* __restrict__ PB, R* UB, R* WB,
                                                   const R* __restrict__ PE, R* UE, R* WE,
                                                   const R* __restrict__ strips, int it, int shot0) {
   VecIdx v;
