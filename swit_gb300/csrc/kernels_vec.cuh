@@ -120,6 +120,10 @@ __device__ __forceinline__ void pdl_enter() {
 }
 
 
+#ifndef SWIT_VEC_REVERSE
+#define SWIT_VEC_REVERSE 1
+#endif
+
 // Task list of a vectorised kernel: entries (ix - 1) << 16 | q, the vectors
 // grouped by the body tier the kernel needs there (the highest over all
 // shots), each group ordered by 2-D tiles for cache locality; entries [0, n0)
@@ -137,10 +141,13 @@ struct VecList {
 // Thread -> (shot, vector, tier) from the list; false past its end.
 template <class R>
 __device__ __forceinline__ bool list_index(const Grid<R>& g, const VecList& L, int shot0, VecIdx& v, int& t) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  // blocks are dispatched about in index order: the last list blocks (tier 2,
+  // the most work) take the lowest block indices, the rectangle the highest
+  const int bx = SWIT_VEC_REVERSE ? (int)(gridDim.x - 1 - blockIdx.x) : (int)blockIdx.x;
+  const int i = bx * blockDim.x + threadIdx.x;
   v.s = shot0 + blockIdx.y;
-  if ((int)blockIdx.x < L.rnb) {  // the tier-0 rectangle, column by column (uniform over the block)
-    const int r = (int)blockIdx.x * blockDim.x + threadIdx.x;
+  if (bx < L.rnb) {  // the tier-0 rectangle, column by column (uniform over the block)
+    const int r = bx * blockDim.x + threadIdx.x;
     if (r >= L.rn) return false;
     const int c = r / L.rnq;
     v.ix = L.rx0 + c + 1;
