@@ -64,40 +64,6 @@ __device__ __forceinline__ R vget(const V4<R>& v, int j) {
   return r;
 }
 
-// Vector of column c (1-based) of a per-shot field, or zeros outside the grid
-// or the column.  Read-only within a launch (double-buffered state, constant
-// coefficients), so the non-coherent path is safe.
-template <class R>
-__device__ __forceinline__ V4<R> ldw(const R* __restrict__ f, int c, int NX, int LD4, int q, bool qok) {
-  V4<R> v;
-  if (qok && c >= 1 && c <= NX) {
-    const size_t k4 = (size_t)(c - 1) * LD4 + q;
-    if constexpr (sizeof(R) == 4) {
-      const float4 t = __ldg(reinterpret_cast<const float4*>(f) + k4);
-      v.x[0] = t.x;
-      v.x[1] = t.y;
-      v.x[2] = t.z;
-      v.x[3] = t.w;
-    } else {
-      const double2 a = __ldg(reinterpret_cast<const double2*>(f) + 2 * k4);
-      const double2 b = __ldg(reinterpret_cast<const double2*>(f) + 2 * k4 + 1);
-      v.x[0] = a.x;
-      v.x[1] = a.y;
-      v.x[2] = b.x;
-      v.x[3] = b.y;
-    }
-  } else {
-#pragma unroll
-    for (int j = 0; j < 4; ++j) v.x[j] = R(0);
-  }
-  return v;
-}
-
-template <class R>
-__device__ __forceinline__ void stw(R* __restrict__ f, int c, int LD4, int q, const V4<R>& v) {
-  st4(f, (size_t)(c - 1) * LD4 + q, v);
-}
-
 // Damping of the rows iz0 .. iz0+4 of one lane along the columns
 // (pml.f90:88-99, damp_at in kernels.cuh): a row in the top or bottom PML has
 // the value v on its trapezoid span [lo, hi]; everywhere else the value is the
@@ -199,21 +165,9 @@ __device__ __forceinline__ void walk_strips(const Grid<R>& g, R* __restrict__ bs
   }
 }
 
-// Records of the receivers in column c whose row lies in this lane's vector
+// Records of the receivers in a column whose row lies in this lane's vector
 // (fdcore.f90:123-128; vx / vz after dev/solver/fdcore.f90:162-175), in
-// receiver order.
-template <class R>
-__device__ __forceinline__ void walk_record(const Grid<R>& g, const Receivers& rec, R* __restrict__ seis_t, int s,
-                                            int it, int c, int iz0, const V4<R>& v) {
-  const int* cp = rec.colptr + (size_t)s * (g.NX + 2);
-  const int e1 = cp[c + 1];
-  for (int e = cp[c]; e < e1; ++e) {
-    const int j = rec.zrow[e] - iz0;
-    if (j >= 0 && j < 4) seis_t[((size_t)s * g.nt + (it - 1)) * g.ngmax + rec.ig[e]] = vget(v, j);
-  }
-}
-
-// The same from the column's table entry rc = rcol[c] (loaded with the
+// receiver order, from the column's table entry rc = rcol[c] (loaded with the
 // iteration's other loads, so the common one-receiver column adds no
 // dependent load).
 template <class R>
