@@ -1637,10 +1637,12 @@ struct swit_multi {
   uint2* d_blocks[4] = {nullptr, nullptr, nullptr, nullptr};  // the waves' block tables, one after another
   int* d_on = nullptr;  // per table row: instance switched on for this call
   // A wave is a group of (instance, shot) pairs, in table order, whose reverse-loop state fits its share of
-  // the L2; waves run their loops on concurrent graph branches.  act[k][s]: active blocks of kernel k at forward
+  // the L2; waves run their loops on concurrent branch streams.  act[k][s]: active blocks of kernel k at forward
   // step s (k = 0, 1) or reverse index s (k = 2, 3).
   struct Wave {
     int max_nt = 0;
+    double state = 0.0;    // reverse-loop bytes of its pairs (the work of one launch)
+    bool graphed = false;  // its loops are captured graphs; otherwise launched step by step on each call
     size_t boff[4] = {0, 0, 0, 0};
     std::vector<int> act[4];
     std::vector<int> rows;         // table rows with a pair in this wave
@@ -1649,6 +1651,7 @@ struct swit_multi {
     cudaGraphExec_t g[3] = {nullptr, nullptr, nullptr};  // its forward (no strips, strips) and reverse loops
   };
   std::vector<Wave> waves;
+  size_t graph_nodes = size_t(1) << 20;  // kernel nodes per loop held in the waves' graphs, at most
   int branches = 3;
   cudaStream_t cap = nullptr, capx[2] = {nullptr, nullptr};
   cudaEvent_t ev_fork = nullptr, ev_join[2] = {nullptr, nullptr};
@@ -1681,8 +1684,10 @@ void multi_release(swit_multi* m) {
 // Instance table, padded task lists, waves with their block tables and active
 // prefixes.  Waves take (instance, shot) pairs in table order (record length,
 // longest first) while their reverse-loop state stays under 0.7 L2 / branches
-// (as the single-instance engine sizes its batches), at most about 1 M kernel
-// nodes per loop over all waves.
+// (as the single-instance engine sizes its batches).  The waves with the least
+// work per launch (where launch overhead weighs most) get captured graphs, up
+// to m->graph_nodes kernel nodes per loop over all waves; the others are
+// launched step by step, interleaved over the branch streams.
 int multi_build(swit_multi* m) {
   const int n = (int)m->eng.size();
   m->order.resize(n);
@@ -1729,8 +1734,8 @@ int multi_build(swit_multi* m) {
         const uint32_t t = i < e->list_n0[k] ? 0u : (i < e->list_n1[k] ? 1u : 2u);
         L.push_back((t << 30) | src[i]);
       }
-      while (L.size() % 256) L.push_back(kMultiPad);
-      chunks[k].push_back((uint32_t)((L.size() - base[k][r]) / 256));
+      while (L.size() % kMultiBlock) L.push_back(kMultiPad);
+      chunks[k].push_back((uint32_t)((L.size() - base[k][r]) / kMultiBlock));
     }
     CK(cudaMalloc(&m->d_list[k], std::max<size_t>(L.size(), 1) * sizeof(uint32_t)));
     CK(cudaMemcpy(m->d_list[k], L.data(), L.size() * sizeof(uint32_t), cudaMemcpyHostToDevice));
@@ -1750,30 +1755,29 @@ int multi_build(swit_multi* m) {
     const double v = std::atof(wb);
     if (v > 0) budget = v;
   }
-  std::vector<std::vector<std::pair<int, int>>> groups;
-  for (int attempt = 0; attempt < 64; ++attempt) {
-    groups.clear();
-    double used = 0.0;
-    for (int r = 0; r < n; ++r)
-      for (int sh = 0; sh < m->eng[m->order[r]]->ns; ++sh) {
-        if (groups.empty() || (used + state[r] > budget && !groups.back().empty())) {
-          groups.emplace_back();
-          used = 0.0;
-        }
-        groups.back().emplace_back(r, sh);
-        used += state[r];
-      }
-    size_t nodes = 0;
-    for (auto& gr : groups) nodes += 2 * (size_t)(m->eng[m->order[gr.front().first]]->nt - 1);
-    if (nodes <= ((size_t)1 << 20) || groups.size() <= (size_t)m->branches) break;
-    budget *= 1.5;
+  if (const char* gn = std::getenv("SWIT_MULTI_GRAPH_NODES")) {  // e.g. 0: every wave launched step by step
+    const long long v = std::atoll(gn);
+    if (v >= 0) m->graph_nodes = (size_t)v;
   }
+  std::vector<std::vector<std::pair<int, int>>> groups;
+  double used = 0.0;
+  for (int r = 0; r < n; ++r)
+    for (int sh = 0; sh < m->eng[m->order[r]]->ns; ++sh) {
+      if (groups.empty() || (used + state[r] > budget && !groups.back().empty())) {
+        groups.emplace_back();
+        used = 0.0;
+      }
+      groups.back().emplace_back(r, sh);
+      used += state[r];
+    }
   std::vector<uint2> B[4];
   for (auto& gr : groups) {
     swit_multi::Wave w;
     w.max_nt = m->eng[m->order[gr.front().first]]->nt;
-    for (auto& pr : gr)
+    for (auto& pr : gr) {
+      w.state += state[pr.first];
       if (w.rows.empty() || w.rows.back() != pr.first) w.rows.push_back(pr.first);
+    }
     if (w.rows.size() == 1) {  // the pairs of one instance are consecutive shots
       w.s0 = gr.front().second;
       w.nb = (int)gr.size();
@@ -1784,7 +1788,7 @@ int multi_build(swit_multi* m) {
       for (auto& pr : gr) {
         const int r = pr.first;
         for (uint32_t c = 0; c < chunks[k][r]; ++c)
-          B[k].push_back(make_uint2(((uint32_t)r << 16) | (uint32_t)pr.second, base[k][r] + 256u * c));
+          B[k].push_back(make_uint2(((uint32_t)r << 16) | (uint32_t)pr.second, base[k][r] + (uint32_t)kMultiBlock * c));
         cum.push_back((int)(B[k].size() - w.boff[k]));
       }
       // pairs whose instance has nt >= s run forward step s and reverse index s - 2: a prefix of the wave
@@ -1801,6 +1805,17 @@ int multi_build(swit_multi* m) {
     }
     m->waves.push_back(std::move(w));
   }
+  std::vector<int> by_work(m->waves.size());
+  for (size_t i = 0; i < by_work.size(); ++i) by_work[i] = (int)i;
+  std::stable_sort(by_work.begin(), by_work.end(),
+                   [&](int a, int b) { return m->waves[a].state < m->waves[b].state; });
+  size_t nodes = 0;
+  for (int i : by_work) {
+    const size_t wn = 2 * (size_t)(m->waves[i].max_nt - 1);
+    if (nodes + wn > m->graph_nodes) break;
+    nodes += wn;
+    m->waves[i].graphed = true;
+  }
   for (int k = 0; k < 4; ++k) {
     CK(cudaMalloc(&m->d_blocks[k], std::max<size_t>(B[k].size(), 1) * sizeof(uint2)));
     CK(cudaMemcpy(m->d_blocks[k], B[k].data(), B[k].size() * sizeof(uint2), cudaMemcpyHostToDevice));
@@ -1815,18 +1830,47 @@ int multi_build(swit_multi* m) {
   return 0;
 }
 
+// Steps [q0, q1) of wave w's forward (which = 0: no strips, 1: with strips) or
+// reverse (which = 2) loop on st; step q is forward step it = q + 2, reverse
+// index jr = q (instance step nt - q).  One launch per phase and step covers
+// every pair of the wave still running.
+void wave_steps(swit_multi* m, swit_multi::Wave& w, int which, int q0, int q1, cudaStream_t st) {
+  if (w.rows.size() == 1) {
+    // one instance: its own single-instance kernels (same bodies, same bits), without
+    // the instance table or the per-instance block padding of the shared kernels
+    swit_engine* e = m->eng[m->order[w.rows[0]]];
+    if (which < 2)
+      launch_forward_steps<float>(e, which == 1, w.s0, w.nb, st, q0 + 2, q1 + 1);
+    else
+      launch_backward_steps<float>(e, w.s0, w.nb, st, e->nt - q0, e->nt - q1 + 1);
+    return;
+  }
+  const dim3 block(kMultiBlock);
+  const Inst<float>* tab = m->d_tab;
+  auto grid = [](int nb) { return dim3((unsigned)std::max(1, nb)); };
+  auto ml = [&](int k, int nb) { return MultiLaunch{m->d_blocks[k] + w.boff[k], m->d_list[k], m->d_on, nb}; };
+  for (int q = q0; q < q1; ++q) {
+    if (which < 2) {
+      const int it = q + 2;
+      launch_pdl(true, k_fwd_p_m<float>, grid(w.act[0][it]), block, st, tab, ml(0, w.act[0][it]), it);
+      launch_pdl(true, k_fwd_uw_m<float>, grid(w.act[1][it]), block, st, tab, ml(1, w.act[1][it]), it, which);
+    } else {
+      launch_pdl(true, k_bwd_uw_m<float>, grid(w.act[2][q]), block, st, tab, ml(2, w.act[2][q]), q);
+      launch_pdl(true, k_bwd_p_m<float>, grid(w.act[3][q]), block, st, tab, ml(3, w.act[3][q]), q);
+    }
+  }
+}
+
 // The forward (which = 0: no strips, 1: with strips) or reverse (which = 2)
-// loop of every switched-on instance.  Each wave's loop (one launch per phase
-// and step) is captured once into a graph of its own; a call launches the
-// graphs of the waves that hold a switched-on instance, spread over the
-// concurrent branch streams.  on[i] (caller order) switches instance i on.
+// loop of every switched-on instance.  A graphed wave's loop is captured once
+// into a graph of its own; a call launches the graphs of the waves that hold a
+// switched-on instance, spread over the concurrent branch streams, and then the
+// other such waves step by step, a few steps per branch in turn so that every
+// branch has work queued.  on[i] (caller order) switches instance i on.
 int multi_loop(swit_multi* m, int which, const std::vector<int>& on, cudaStream_t st) {
   std::vector<int> rows(m->eng.size());
   for (size_t r = 0; r < rows.size(); ++r) rows[r] = on[m->order[r]];
   CK(cudaMemcpyAsync(m->d_on, rows.data(), rows.size() * sizeof(int), cudaMemcpyHostToDevice, st));
-  const dim3 block(256);
-  const Inst<float>* tab = m->d_tab;
-  auto grid = [](int nb) { return dim3((unsigned)std::max(1, nb)); };
   std::vector<int> active;
   for (int wi = 0; wi < (int)m->waves.size(); ++wi)
     for (int r : m->waves[wi].rows)
@@ -1836,30 +1880,10 @@ int multi_loop(swit_multi* m, int which, const std::vector<int>& on, cudaStream_
       }
   for (int wi : active) {
     swit_multi::Wave& w = m->waves[wi];
-    if (w.g[which]) continue;
+    if (!w.graphed || w.g[which]) continue;
     cudaError_t rc = cudaStreamBeginCapture(m->cap, cudaStreamCaptureModeThreadLocal);
     if (rc != cudaSuccess) return fail(SWIT_E_CUDA, "multi-instance graph capture: %s", cudaGetErrorString(rc));
-    auto ml = [&](int k, int nb) { return MultiLaunch{m->d_blocks[k] + w.boff[k], m->d_list[k], m->d_on, nb}; };
-    if (w.rows.size() == 1) {
-      // one instance: its own single-instance kernels (same bodies, same bits), without
-      // the instance table or the per-instance block padding of the shared kernels
-      swit_engine* e = m->eng[m->order[w.rows[0]]];
-      if (which < 2)
-        launch_forward_steps<float>(e, which == 1, w.s0, w.nb, m->cap);
-      else
-        launch_backward_steps<float>(e, w.s0, w.nb, m->cap);
-    } else if (which < 2) {
-      for (int it = 2; it <= w.max_nt; ++it) {
-        launch_pdl(true, k_fwd_p_m<float>, grid(w.act[0][it]), block, m->cap, tab, ml(0, w.act[0][it]), it);
-        launch_pdl(true, k_fwd_uw_m<float>, grid(w.act[1][it]), block, m->cap, tab, ml(1, w.act[1][it]), it,
-                   which);
-      }
-    } else {
-      for (int jr = 0; jr <= w.max_nt - 2; ++jr) {
-        launch_pdl(true, k_bwd_uw_m<float>, grid(w.act[2][jr]), block, m->cap, tab, ml(2, w.act[2][jr]), jr);
-        launch_pdl(true, k_bwd_p_m<float>, grid(w.act[3][jr]), block, m->cap, tab, ml(3, w.act[3][jr]), jr);
-      }
-    }
+    wave_steps(m, w, which, 0, w.max_nt - 1, m->cap);
     cudaGraph_t graph = nullptr;
     rc = cudaStreamEndCapture(m->cap, &graph);
     if (rc == cudaSuccess) {
@@ -1873,12 +1897,35 @@ int multi_loop(swit_multi* m, int which, const std::vector<int>& on, cudaStream_
   }
   // the waves on the branch streams, forked from and joined back to st
   const int br = std::max(1, std::min(m->branches, (int)active.size()));
+  auto branch = [&](int b) { return b ? m->capx[b - 1] : st; };
   CK(cudaEventRecord(m->ev_fork, st));
   for (int i = 0; i < br - 1; ++i) CK(cudaStreamWaitEvent(m->capx[i], m->ev_fork, 0));
-  for (size_t k = 0; k < active.size(); ++k) {
-    const int b = (int)(k % br);
-    CK(cudaGraphLaunch(m->waves[active[k]].g[which], b ? m->capx[b - 1] : st));
+  std::vector<std::vector<int>> direct(br);
+  int k = 0;
+  for (int wi : active)
+    if (m->waves[wi].graphed) CK(cudaGraphLaunch(m->waves[wi].g[which], branch(k++ % br)));
+  for (int wi : active)
+    if (!m->waves[wi].graphed) direct[k++ % br].push_back(wi);
+  // per branch: position (wave, next step) in its list of directly launched waves
+  constexpr int kStepsPerTurn = 8;
+  std::vector<size_t> wpos(br, 0);
+  std::vector<int> qpos(br, 0);
+  for (bool more = true; more;) {
+    more = false;
+    for (int b = 0; b < br; ++b) {
+      if (wpos[b] >= direct[b].size()) continue;
+      swit_multi::Wave& w = m->waves[direct[b][wpos[b]]];
+      const int q1 = std::min(w.max_nt - 1, qpos[b] + kStepsPerTurn);
+      wave_steps(m, w, which, qpos[b], q1, branch(b));
+      qpos[b] = q1;
+      if (q1 == w.max_nt - 1) {
+        ++wpos[b];
+        qpos[b] = 0;
+      }
+      more = true;
+    }
   }
+  CK(cudaGetLastError());
   for (int i = 0; i < br - 1; ++i) {
     CK(cudaEventRecord(m->ev_join[i], m->capx[i]));
     CK(cudaStreamWaitEvent(st, m->ev_join[i], 0));

@@ -4,7 +4,7 @@
 // Each instance is a regular engine (its own arrays); a device table holds per
 // instance the grid description, receiver and source tables and array
 // pointers.  Per phase kernel, every instance's own task list (kernels_vec.cuh)
-// is padded to whole blocks of 256 entries and the blocks of a wave's
+// is padded to whole blocks of kMultiBlock entries and the blocks of a wave's
 // (instance, shot) pairs are listed in the wave's block table, instances ordered
 // by record length nt, longest first.  Within a wave all forward loops start
 // together and all reverse loops start together, so at a given step the blocks
@@ -32,6 +32,12 @@ struct Inst {
 };
 
 constexpr uint32_t kMultiPad = 0xffffffffu;  // padding entry of a block
+// Threads (list entries) per block of the multi-instance kernels. 128-entry blocks
+// (as the single-instance vec kernels use) measured no faster on uneven batches.
+#ifndef SWIT_MULTI_BLOCK
+#define SWIT_MULTI_BLOCK 256
+#endif
+constexpr int kMultiBlock = SWIT_MULTI_BLOCK;
 
 // Block table entry: x = instance << 16 | shot, y = first list entry of the block.
 // List entries: tier << 30 | (ix - 1) << 16 | q, or kMultiPad.
@@ -89,13 +95,13 @@ __device__ __forceinline__ void multi_vec(const int LD, uint32_t e, int s, VecId
 
 // Forward phases at step it (the same step for every running instance).
 template <class R>
-__global__ void __launch_bounds__(256) k_fwd_p_m(const Inst<R>* __restrict__ tab, MultiLaunch L, int it) {
+__global__ void __launch_bounds__(kMultiBlock) k_fwd_p_m(const Inst<R>* __restrict__ tab, MultiLaunch L, int it) {
   SWIT_MULTI_PROLOGUE
   SWIT_TIER_CALL(fwd_p_body, I->g, I->src, I->s_fwd, I->p + off, I->u + off, I->w + off, it, v);
 }
 
 template <class R>
-__global__ void __launch_bounds__(256) k_fwd_uw_m(const Inst<R>* __restrict__ tab, MultiLaunch L, int it, int store) {
+__global__ void __launch_bounds__(kMultiBlock) k_fwd_uw_m(const Inst<R>* __restrict__ tab, MultiLaunch L, int it, int store) {
   SWIT_MULTI_PROLOGUE
   SWIT_TIER_CALL(fwd_uw_body, I->g, I->rec, I->p + off, I->u + off, I->w + off, I->seis_t, store ? I->strips : nullptr,
                  it, v);
@@ -103,14 +109,14 @@ __global__ void __launch_bounds__(256) k_fwd_uw_m(const Inst<R>* __restrict__ ta
 
 // Reverse phases at reverse index jr: instance step it = nt - jr.
 template <class R>
-__global__ void __launch_bounds__(256) k_bwd_uw_m(const Inst<R>* __restrict__ tab, MultiLaunch L, int jr) {
+__global__ void __launch_bounds__(kMultiBlock) k_bwd_uw_m(const Inst<R>* __restrict__ tab, MultiLaunch L, int jr) {
   SWIT_MULTI_PROLOGUE
   SWIT_TIER_CALL(bwd_uw_body, I->g, I->pb + off, I->ub + off, I->wb + off, I->pe + off, I->ue + off, I->we + off,
                  I->strips, I->g.nt - jr, v);
 }
 
 template <class R>
-__global__ void __launch_bounds__(256) k_bwd_p_m(const Inst<R>* __restrict__ tab, MultiLaunch L, int jr) {
+__global__ void __launch_bounds__(kMultiBlock) k_bwd_p_m(const Inst<R>* __restrict__ tab, MultiLaunch L, int jr) {
   SWIT_MULTI_PROLOGUE
   SWIT_TIER_CALL(bwd_p_body, I->g, I->rec, I->src, I->s_fwd, I->adj_t, I->pb + off, I->ub + off, I->wb + off,
                  I->pe + off, I->ue + off, I->we + off, I->dg + off, I->dfw + off, I->dbk + off, I->strips,

@@ -164,16 +164,20 @@ def _uneven_problems():
     return out
 
 
-@pytest.mark.parametrize("wave_bytes", [None, "1", "3e6"])
-def test_multi_engine_matches_each_engine_bit_for_bit(wave_bytes, monkeypatch):
+@pytest.mark.parametrize("wave_bytes,graph_nodes", [(None, None), ("1", None), ("3e6", None), ("1", "0"),
+                                                     ("3e6", "0"), ("1", "700")])
+def test_multi_engine_matches_each_engine_bit_for_bit(wave_bytes, graph_nodes, monkeypatch):
     """All problems stepped by shared launches give each problem's own engine's
     seismogram misfit, gradient and illuminations exactly, twice in a row; also
-    with one (problem, shot) pair per wave on the concurrent branches, and with
-    waves of a few pairs."""
+    with one (problem, shot) pair per wave on the concurrent branches, with
+    waves of a few pairs, and with waves launched step by step instead of as
+    graphs (all of them, or those beyond a small graph node budget)."""
     import torch
     from swit_gb300 import MultiEngine
     if wave_bytes:
         monkeypatch.setenv("SWIT_MULTI_WAVE_BYTES", wave_bytes)
+    if graph_nodes:
+        monkeypatch.setenv("SWIT_MULTI_GRAPH_NODES", graph_nodes)
     surveys = _uneven_problems()
     ref = []
     for s in surveys:
