@@ -1642,6 +1642,7 @@ struct swit_multi {
   struct Wave {
     int max_nt = 0;
     double state = 0.0;    // reverse-loop bytes of its pairs (the work of one launch)
+    double work = 0.0;     // state bytes x steps summed over its pairs (the work of one loop)
     bool graphed = false;  // its loops are captured graphs; otherwise launched step by step on each call
     size_t boff[4] = {0, 0, 0, 0};
     std::vector<int> act[4];
@@ -1776,6 +1777,7 @@ int multi_build(swit_multi* m) {
     w.max_nt = m->eng[m->order[gr.front().first]]->nt;
     for (auto& pr : gr) {
       w.state += state[pr.first];
+      w.work += state[pr.first] * (m->eng[m->order[pr.first]]->nt - 1);
       if (w.rows.empty() || w.rows.back() != pr.first) w.rows.push_back(pr.first);
     }
     if (w.rows.size() == 1) {  // the pairs of one instance are consecutive shots
@@ -1863,10 +1865,11 @@ void wave_steps(swit_multi* m, swit_multi::Wave& w, int which, int q0, int q1, c
 
 // The forward (which = 0: no strips, 1: with strips) or reverse (which = 2)
 // loop of every switched-on instance.  A graphed wave's loop is captured once
-// into a graph of its own; a call launches the graphs of the waves that hold a
-// switched-on instance, spread over the concurrent branch streams, and then the
-// other such waves step by step, a few steps per branch in turn so that every
-// branch has work queued.  on[i] (caller order) switches instance i on.
+// into a graph of its own.  A call spreads the waves that hold a switched-on
+// instance over the concurrent branch streams, largest first onto the least
+// loaded branch, launches the graphs, and then the other waves step by step, a
+// few steps per branch in turn so that every branch has work queued.  on[i]
+// (caller order) switches instance i on.
 int multi_loop(swit_multi* m, int which, const std::vector<int>& on, cudaStream_t st) {
   std::vector<int> rows(m->eng.size());
   for (size_t r = 0; r < rows.size(); ++r) rows[r] = on[m->order[r]];
@@ -1900,12 +1903,19 @@ int multi_loop(swit_multi* m, int which, const std::vector<int>& on, cudaStream_
   auto branch = [&](int b) { return b ? m->capx[b - 1] : st; };
   CK(cudaEventRecord(m->ev_fork, st));
   for (int i = 0; i < br - 1; ++i) CK(cudaStreamWaitEvent(m->capx[i], m->ev_fork, 0));
+  std::vector<int> by_work = active;
+  std::stable_sort(by_work.begin(), by_work.end(),
+                   [&](int a, int b) { return m->waves[a].work > m->waves[b].work; });
+  std::vector<double> load(br, 0.0);
   std::vector<std::vector<int>> direct(br);
-  int k = 0;
-  for (int wi : active)
-    if (m->waves[wi].graphed) CK(cudaGraphLaunch(m->waves[wi].g[which], branch(k++ % br)));
-  for (int wi : active)
-    if (!m->waves[wi].graphed) direct[k++ % br].push_back(wi);
+  for (int wi : by_work) {
+    const int b = (int)(std::min_element(load.begin(), load.end()) - load.begin());
+    load[b] += m->waves[wi].work;
+    if (m->waves[wi].graphed)
+      CK(cudaGraphLaunch(m->waves[wi].g[which], branch(b)));
+    else
+      direct[b].push_back(wi);
+  }
   // per branch: position (wave, next step) in its list of directly launched waves
   constexpr int kStepsPerTurn = 8;
   std::vector<size_t> wpos(br, 0);
