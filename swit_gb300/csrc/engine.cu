@@ -1683,9 +1683,9 @@ void multi_release(swit_multi* m) {
 }
 
 // Instance table, padded task lists, waves with their block tables and active
-// prefixes.  Waves take (instance, shot) pairs in table order (record length,
-// longest first) while their reverse-loop state stays under 0.7 L2 / branches
-// (as the single-instance engine sizes its batches).  The waves with the least
+// prefixes.  A wave's reverse-loop state stays under 0.7 L2 / branches (as the
+// single-instance engine sizes its batches); its (instance, shot) pairs are in
+// table order (record length, longest first).  The waves with the least
 // work per launch (where launch overhead weighs most) get captured graphs, up
 // to m->graph_nodes kernel nodes per loop over all waves; the others are
 // launched step by step, interleaved over the branch streams.
@@ -1760,17 +1760,33 @@ int multi_build(swit_multi* m) {
     const long long v = std::atoll(gn);
     if (v >= 0) m->graph_nodes = (size_t)v;
   }
-  std::vector<std::vector<std::pair<int, int>>> groups;
+  // A problem's shots form waves of their own, equal parts of at most budget / state shots (so that its
+  // waves run its single-instance kernels; fewer, larger waves than the engine's own batches, which spread
+  // one problem over the branches); problems whose shots all fit in half the budget share waves with the
+  // next such problems, in table order (the shared kernels).
+  std::vector<std::vector<std::pair<int, int>>> groups, shared(1);
   double used = 0.0;
-  for (int r = 0; r < n; ++r)
-    for (int sh = 0; sh < m->eng[m->order[r]]->ns; ++sh) {
-      if (groups.empty() || (used + state[r] > budget && !groups.back().empty())) {
-        groups.emplace_back();
+  for (int r = 0; r < n; ++r) {
+    const int ns = m->eng[m->order[r]]->ns;
+    if (ns * state[r] <= 0.5 * budget) {
+      if (used + ns * state[r] > budget && !shared.back().empty()) {
+        shared.emplace_back();
         used = 0.0;
       }
-      groups.back().emplace_back(r, sh);
-      used += state[r];
+      for (int sh = 0; sh < ns; ++sh) shared.back().emplace_back(r, sh);
+      used += ns * state[r];
+      continue;
     }
+    const int per = std::max(1, (int)std::min<double>(ns, budget / state[r]));
+    const int nw = (ns + per - 1) / per;
+    for (int i = 0; i < nw; ++i) {
+      groups.emplace_back();
+      for (int sh = (int)((long long)ns * i / nw); sh < (int)((long long)ns * (i + 1) / nw); ++sh)
+        groups.back().emplace_back(r, sh);
+    }
+  }
+  for (auto& gr : shared)
+    if (!gr.empty()) groups.push_back(std::move(gr));
   std::vector<uint2> B[4];
   for (auto& gr : groups) {
     swit_multi::Wave w;

@@ -164,14 +164,16 @@ def _uneven_problems():
     return out
 
 
-@pytest.mark.parametrize("wave_bytes,graph_nodes", [(None, None), ("1", None), ("3e6", None), ("1", "0"),
-                                                     ("3e6", "0"), ("1", "700")])
+@pytest.mark.parametrize("wave_bytes,graph_nodes", [(None, None), ("1", None), ("5e5", None), ("1", "0"),
+                                                     ("5e5", "0"), ("1", "700")])
 def test_multi_engine_matches_each_engine_bit_for_bit(wave_bytes, graph_nodes, monkeypatch):
     """All problems stepped by shared launches give each problem's own engine's
-    seismogram misfit, gradient and illuminations exactly, twice in a row; also
-    with one (problem, shot) pair per wave on the concurrent branches, with
-    waves of a few pairs, and with waves launched step by step instead of as
-    graphs (all of them, or those beyond a small graph node budget)."""
+    seismogram misfit, gradient and illuminations exactly, twice in a row.
+    Wave layouts: the three small problems in one shared wave (default); one
+    (problem, shot) pair per wave (wave budget 1 byte); a wave of one problem
+    beside a wave shared by two (5e5 bytes); and waves launched step by step
+    instead of as graphs (all of them, or those beyond a small graph node
+    budget)."""
     import torch
     from swit_gb300 import MultiEngine
     if wave_bytes:
