@@ -273,10 +273,13 @@ int swit_misfit_l2(swit_engine* e, const float* src, const float* obs, double* m
  * A multi-instance engine holds n regular engines (one swit_desc each: FP32,
  * batched path, vec kernels, boundary saving; grids, shot counts and nt may all
  * differ) and steps them together: the (instance, shot) pairs are grouped
- * into L2-sized waves, and per wave each time step launches the four phase
- * kernels once over every pair still running; the waves run on concurrent
- * branches, and a call runs only the waves holding a switched-on instance
- * (swit_multi_misfit_l2's `active`).  The reference runs one
+ * into L2-sized waves (an instance's own shots, or several small instances),
+ * and per wave each time step launches the phase kernels once over every pair
+ * still running; the waves run on concurrent branches, and a call runs only
+ * the waves holding a switched-on instance (swit_multi_misfit_l2's `active`).
+ * Waves beyond a graph node budget are launched step by step, so a call with
+ * many of them returns only once most of their launches are queued (the host
+ * waits for room in the launch queues).  The reference runs one
  * fd2dmpi job per problem; this has no counterpart there.  Models are set per
  * instance through the handles of swit_multi_engine, which stay owned by the
  * multi-instance engine. */
