@@ -259,7 +259,8 @@ inline BandList band_list(const swit_engine* e, int k) {
                   e->band_stride, e->band_bc, e->band_wait};
 }
 
-// Vec kernels: 256 threads per block over the kernel's task list k, nb shots.
+// Vec kernels: SWIT_VEC_BLOCK threads per block over the kernel's task list k (the tier-0
+// rectangle first, mapped arithmetically, then the device list), nb shots.
 inline VecList vec_list(const swit_engine* e, int k) {
   return VecList{e->d_dlist + (size_t)k * e->list_stride, e->dl_n0[k], e->dl_n1[k], e->dl_len[k], e->rect_x0[k],
                  e->rect_q0[k], e->rect_nq[k], e->rect_n[k], (e->rect_n[k] + SWIT_VEC_BLOCK - 1) / SWIT_VEC_BLOCK};
