@@ -270,9 +270,10 @@ class Engine:
 
 class MultiEngine:
     """Many independent problems (grids, shot counts, record lengths may all
-    differ) stepped together: (problem, shot) pairs in L2-sized waves on
-    concurrent branches, per wave one launch of each phase kernel per time step
-    over the pairs still running (swit_multi_*).  ``problems`` is a list
+    differ) stepped together: (problem, shot) pairs in L2-sized waves (a
+    problem's own shots, or several small problems) on concurrent branches, per
+    wave one launch of each phase kernel per time step over the pairs still
+    running (swit_multi_*).  ``problems`` is a list
     of Engine keyword dicts (nx, nz, npml, nt, dx, dt, src_xz, rec_xz[, ng,
     free_surface, block_x]); ``engines[i]`` is problem i's Engine (set_model,
     forward, ... work on it alone)."""
