@@ -149,6 +149,38 @@ def test_create_rejects_bad_descriptions_before_any_gpu_work(over, code):
     assert lib.swit_last_error().decode()
 
 
+@pytest.mark.parametrize("over,code,text", [
+    (dict(precision=1), -1, "FP32 vec kernels"), (dict(path=1), -1, "FP32 vec kernels"),
+    (dict(kernel_variant=1), -1, "FP32 vec kernels"), (dict(checkpoint_every=10), -1, "boundary saving"),
+    (dict(adjoint_mode=1), -1, "FP32 vec kernels"), (dict(receiver_component=1), -1, "FP32 vec kernels"),
+    (dict(nx=16400), -8, "16384 PML-grid columns"),
+])
+def test_multi_create_rejects_unsupported_problems_before_any_gpu_work(over, code, text):
+    """A multi-instance engine runs FP32 vec kernels on the batched path with
+    boundary saving; any other description, in any position, is refused with
+    its index before an engine is created."""
+    lib = _lib.load()
+    s = survey.small()
+    good, keep0 = _desc(s)
+    bad, keep1 = _desc(s, **over)
+    descs = (_lib.SwitDesc * 2)(good, bad)
+    h = C.c_void_p()
+    assert lib.swit_multi_create(descs, 2, C.byref(h)) == code
+    msg = lib.swit_last_error().decode()
+    assert "instance 1" in msg and text in msg, msg
+    assert not h.value
+
+
+def test_multi_create_rejects_an_empty_batch():
+    lib = _lib.load()
+    h = C.c_void_p()
+    s = survey.small()
+    d, keep = _desc(s)
+    assert lib.swit_multi_create(None, 1, C.byref(h)) == -1
+    assert lib.swit_multi_create(C.byref(d), 0, C.byref(h)) == -1
+    assert lib.swit_multi_destroy(None) == 0
+
+
 def test_create_rejects_receivers_outside_the_model():
     lib = _lib.load()
     s = survey.small()

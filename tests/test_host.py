@@ -86,6 +86,16 @@ def test_engine_rejects_unknown_options_before_any_gpu_work(kw):
         Engine(**s.engine_args(), **kw)
 
 
+@pytest.mark.parametrize("kw", [dict(precision="fp64"), dict(path="plain"), dict(checkpoint_every=100)])
+def test_multi_engine_refuses_problems_it_cannot_batch_before_any_gpu_work(kw):
+    """A MultiEngine runs FP32 problems on the batched path with boundary
+    saving; another problem in the list is refused before the C library sees it."""
+    from swit_gb300 import MultiEngine, survey
+    s = survey.small()
+    with pytest.raises(ValueError, match="FP32 problems on the batched path"):
+        MultiEngine([s.engine_args(), dict(s.engine_args(), **kw)])
+
+
 def test_engine_keeps_pinned_float32_host_buffers():
     """Host float32 inputs reach the C ABI without a copy: a pinned buffer stays
     pinned, so the engine's host-to-device copy is one DMA."""
