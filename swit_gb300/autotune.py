@@ -16,7 +16,7 @@ from .engine import Engine
 _cache = {}
 
 
-def candidates(ns, nz_pml=None):
+def candidates(ns):
     """Launch configurations to time for ns shots: the vec kernels with the
     engine's automatic choice (L2-sized batches on three branches), then 1..8
     batches on 1..4 concurrent graph branches (no more branches than batches).

@@ -107,3 +107,20 @@ def test_engine_keeps_pinned_float32_host_buffers():
     assert Engine._f32(b).ctypes.data == b.ctypes.data
     c = Engine._f32(np.arange(12, dtype=np.float64))
     assert c.dtype == np.float32 and c.flags.c_contiguous
+
+
+@pytest.mark.parametrize("ns", [1, 5, 49, 200])
+def test_autotune_candidates_are_vec_launch_shapes_that_cover_every_shot(ns):
+    """The tuner times the engine's automatic choice first, then vec batches
+    that split ns shots into 1..8 launches on 1..4 branches, never more
+    branches than batches; every candidate covers all shots."""
+    from swit_gb300.autotune import candidates
+    cs = candidates(ns)
+    assert cs[0] == dict(kernel="vec", block_x=4, shots_per_batch=0, graph_branches=0)
+    assert all(c["kernel"] == "vec" for c in cs)
+    assert len({tuple(sorted(c.items())) for c in cs}) == len(cs)
+    for c in cs[1:]:
+        b, br = c["shots_per_batch"], c["graph_branches"]
+        nbatch = -(-ns // b)
+        assert 1 <= b <= ns and 1 <= nbatch <= 8
+        assert br == 1 or br <= nbatch
